@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Throughput of the PyRDSim simulation step on GB300 (particle-steps/s).
+
+Workload (default): the 2D active wall fluid -- N = 65,536 particles at
+density 0.4, periodic in x, reflecting in y, WCA between inactive particles,
+LJ (cut 2.5) between active ones, a 9-3 wall attracting active particles to
+y = 0, activation at rate 0.1 and deactivation at rate 1.0 per active
+neighbour within 1.5.  dt = 1e-4, forces float32, positions 64-bit fixed
+point, counter-based Philox noise.  Synthetic, seeded input.
+
+One bench step = one segment of 1,000 integration steps (the workload's
+20,000 steps are 20 bench steps).  The state (a few MB) is L2-resident
+between integration steps by construction; L2 is flushed (256 MB write)
+between timed segments.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank runs an independent replica (replicas only: the
+single-system path has no data-path exchange), and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300 (active wall fluid, N=65,536)"
+UNIT = "particle-steps/s"
+SEGMENT = 1000
+ALG_BYTES = 40  # per particle-step: 16 B read x, 16 B write x, 4 B type read, 4 B type write
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=65536)
+    p.add_argument("--segment", type=int, default=SEGMENT)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if _has_cuda() else "gloo")
+    return rank, ws, local
+
+
+def _has_cuda():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if _has_cuda() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except Exception:
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def traffic_per_launch(n):
+    """dram bytes per k_force launch from the committed ncu summary (scaled by
+    particles if the capture was a smaller case), or None."""
+    path = os.path.join(ROOT, "profiles", "k_force_active_wall_fluid.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_particle:"):
+                    return float(line.split(":")[1]) * n
+    except Exception:
+        pass
+    return None
+
+
+def cpu_baseline(workload, n_gpu_state=None):
+    """Reference (compiled PyRDSim) on a bounded sample, one core."""
+    from oracle import ref_bench
+    kind = "reference" if ref_bench.reference_available() else "port"
+    n, steps = (4096, 20) if kind == "reference" else (65536, 20)
+    secs = ref_bench.run_sample(kind, workload, n, steps, 5)
+    return {
+        "value": n * steps / secs, "unit": UNIT, "cores": 1, "kind": kind,
+        "sample": (f"{workload} shape at N={n} (density 0.4, tanh wall in place of the "
+                   f"9-3 wall), {steps} integration steps incl. {steps // 10} neighbour "
+                   f"rebuilds, set-up excluded, {secs:.2f} s") if kind == "reference" else
+                  (f"float64 oracle port, {workload} N={n}, {steps} steps, {secs:.2f} s"),
+    }
+
+
+def force_error(eng, sd):
+    """Drift of the GPU engine vs the float64 oracle on the same state."""
+    import numpy as np
+    from oracle.oracle import Oracle
+    x, t = eng.state()
+    eng.set_state(x, t)
+    o = Oracle(sd, history_quirk=False)
+    o.set_state(x, t)
+    a, r = eng.drift(), o.drift()
+    norm = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    mag = np.linalg.norm(r, axis=1)
+    floor = float(np.sqrt(np.mean(mag ** 2)))
+    per = float((np.linalg.norm(a - r, axis=1) / np.maximum(mag, floor)).max())
+    return {"norm": norm, "per_particle_rms_floor": per}
+
+
+def run_ours(args, rank, ws, local):
+    import numpy as np
+    import torch
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    torch.cuda.set_device(local)
+    sd = workloads.active_wall_fluid(n=args.n, seed=2 + rank)
+    eng = Engine([sd], device=local)
+    N, seg = sd.n_particles, args.segment
+    stream = torch.cuda.ExternalStream(eng.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    x0, t0 = eng.state()
+    for _ in range(args.warmup):
+        eng.step(seg)
+    torch.cuda.synchronize()
+    eng.profile()  # reset counters
+    barrier(ws)
+    clocks = ClockSampler(local) if rank == 0 else None
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        starts[k].record(stream)
+        eng.step(seg)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop() if clocks else None
+    prof_counts = eng.profile()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms_max = max_over_ranks(ms, ws)
+    value = ws * N * seg * args.steps / (ms_max / 1e3)
+    launches = sum(v["launches"] for k, v in prof_counts.items() if k != "hook")
+    # roofline pass: per-kernel CUDA events on the engine stream
+    eng.set_profiling(True)
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        eng.step(seg)
+    torch.cuda.synchronize()
+    prof = eng.profile()
+    eng.set_profiling(False)
+    f_ms = prof["force"]["ms"] / max(1, prof["force"]["timed"])
+    r_ms = prof["react"]["ms"] / max(1, prof["react"]["timed"])
+    peak, peak_kind = peaks()
+    achieved = ALG_BYTES * N / (f_ms / 1e3) / 1e9
+    traffic = traffic_per_launch(N)
+    # end to end through the C ABI with host buffers: state in, segment, state out
+    xh = torch.empty((N, 2), dtype=torch.float64, pin_memory=True).numpy()
+    th = torch.empty((N,), dtype=torch.int32, pin_memory=True).numpy()
+    xh[:] = x0
+    th[:] = t0
+    e2e_t = 0.0
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        eng.set_state(xh, th)
+        eng.step(seg)
+        xo, to = eng.state()
+        torch.cuda.synchronize()
+        e2e_t += time.perf_counter() - w0
+    e2e_t = max_over_ranks(e2e_t, ws)
+    e2e = ws * N * seg * args.steps / e2e_t
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 forces, i64 fixed-point x, f64 rates",
+        "data": "synthetic (seeded jittered lattice, 50/50 species)",
+        "config": {"workload": "active_wall_fluid", "n_particles": N, "density": 0.4,
+                   "integration_steps_per_step": seg, "dt": 1e-4,
+                   "boundaries": "periodic x, reflecting y", "noise": "Philox4x32-10",
+                   "l2": "flushed (256 MB write) between timed steps; state L2-resident "
+                         "within a step", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(N * 2 * 8 + N * 4),
+                "d2h_bytes_per_step": int(N * 2 * 8 + N * 4),
+                "path": "C ABI: rdsim_set_state (host) + rdsim_step + rdsim_get_state (host)"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_force<2,4>",
+                     "algorithmic_bytes_per_launch": ALG_BYTES * N,
+                     "avg_launch_us": f_ms * 1e3, "peak_source": peak_kind,
+                     "react_avg_launch_us": r_ms * 1e3},
+        "kernel_ms": {k: v["ms"] for k, v in prof.items()},
+        "kernel_launches": {k: v["launches"] for k, v in prof.items()},
+        "clocks": clk,
+        "engine": eng.info(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        try:
+            out["cpu_baseline"] = cpu_baseline("active_wall_fluid")
+        except Exception as exc:
+            out["cpu_baseline"] = {"unavailable": str(exc)[:200]}
+        try:
+            out["force_err_vs_fp64"] = force_error(eng, sd)
+        except Exception as exc:
+            out["force_err_vs_fp64"] = {"unavailable": str(exc)[:200]}
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def _ref_worker(a):
+    from oracle import ref_bench
+    kind, workload, n, steps, seed = a
+    return ref_bench.run_sample(kind, workload, n, steps, seed)
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import ref_bench
+    kind = "reference" if ref_bench.reference_available() else "port"
+    n, steps = (4096, 10) if kind == "reference" else (65536, 5)
+    procs = max(1, min(16, os.cpu_count() or 1))
+    ctx = mp.get_context("spawn")
+    total_ps, total_t = 0.0, 0.0
+    with ctx.Pool(procs) as pool:
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            secs = pool.map(_ref_worker, [(kind, "active_wall_fluid", n, steps, 100 * k + p)
+                                          for p in range(procs)])
+            if k >= args.warmup:
+                total_ps += procs * n * steps
+                total_t += max(secs)
+    value = total_ps / total_t
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded jittered lattice, 50/50 species)",
+        "config": {"workload": "active_wall_fluid", "n_particles": n, "density": 0.4,
+                   "integration_steps_per_step": steps, "dt": 1e-4,
+                   "parallelism": f"{procs} independent single-threaded processes"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": kind,
+                         "sample": f"{procs} processes x N={n} (tanh wall for the 9-3 wall), "
+                                   f"{steps} integration steps each per step, set-up excluded"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank, ws, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_ours(args, rank, ws, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -229,6 +229,21 @@ typedef struct {
 } rdsim_info;
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 
+/* Kernel accounting (no reference counterpart; measurement only).  Launch
+ * counts are always kept; with profiling enabled every kernel launch is also
+ * bracketed by CUDA events on the handle's stream and its device time summed
+ * per class: 0 = drift (k_force), 1 = reactions (k_react), 2 = stand-alone
+ * Euler-Maruyama (k_em), 3 = cell-list rebuild (5 kernels), 4 = hooks. */
+#define RDSIM_PROFILE_CLASSES 5
+typedef struct {
+  int64_t launches[RDSIM_PROFILE_CLASSES];
+  double ms[RDSIM_PROFILE_CLASSES];
+  int64_t timed[RDSIM_PROFILE_CLASSES];
+} rdsim_profile;
+int rdsim_set_profiling(rdsim_handle* h, int32_t enable);
+/* Fills *p and resets the counters (synchronises the stream). */
+int rdsim_get_profile(rdsim_handle* h, rdsim_profile* p);
+
 /* Message of the last failing call on this thread. */
 const char* rdsim_last_error(void);
 

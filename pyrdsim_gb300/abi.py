@@ -119,6 +119,16 @@ class Info(C.Structure):
                 ("device_bytes", C.c_int64)]
 
 
+PROFILE_CLASSES = 5
+PROFILE_NAMES = ["force", "react", "em", "rebuild", "hook"]
+
+
+class Profile(C.Structure):
+    _fields_ = [("launches", C.c_int64 * PROFILE_CLASSES),
+                ("ms", C.c_double * PROFILE_CLASSES),
+                ("timed", C.c_int64 * PROFILE_CLASSES)]
+
+
 def dptr(a):
     """Pointer to a contiguous float64 numpy array (or None)."""
     if a is None:

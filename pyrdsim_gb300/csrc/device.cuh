@@ -1,0 +1,191 @@
+// device.cuh -- data layout and device helpers of the GB300 step engine.
+//
+// Layout in HBM (all per-particle arrays in *cell-sorted* order, systems
+// concatenated; re-sorted at every neighbour-list rebuild):
+//   xh[buf][k][i]  u32  high word of the 64-bit fixed-point coordinate k
+//   xl[buf][k][i]  u32  low word
+//   meta[buf][i]   u32  type | type_at_rebuild << 8 | local atom << 16 |
+//                       template << 24 (0xff = no bonded terms)
+//   mol[buf][i]    i32  molecule number (initial-condition column 0)
+//   pid[buf][i]    i32  particle index in the caller's order
+// Fixed point per dimension k of a system with box length L:
+//   periodic   : X in [0, 2^64) represents X * L / 2^64 (wraps exactly)
+//   reflecting : X in [0, S], S = 2^63 - 2^34, represents X * L / S
+// The pair kernels use only the high words: (int32)(hj - hi) * unit_hi is
+// the minimum-image displacement in float32 for periodic dimensions and the
+// plain displacement for reflecting ones.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/rdsim.h"
+
+namespace rd {
+
+constexpr int MAXT = RDSIM_MAX_TYPES;
+constexpr int MAXI = RDSIM_MAX_INTERACTIONS;
+constexpr int MAXR = RDSIM_MAX_REACTIONS;
+constexpr int MAXA = RDSIM_MAX_ATOMS;
+constexpr int MAXW = 8;          // wall interactions per system
+constexpr int MAXHC = 256;       // halo cells per tile
+constexpr int BLOCK = 128;       // threads per CTA of the tile kernels
+
+// One nonbonded pair law in evaluation form (pyrdsim.pyx:1068-1130).
+struct PairLaw {
+  int law, n;
+  float c0, c1, c2, c3;           // law constants, see eval_pair()
+  float rc2_lo, rc2_hi;           // guard band around rc^2 (exact check inside)
+  float in2_lo, in2_hi;           // piecewise_linear: guard band around (r0-dr)^2
+  double rc, rin;                 // exact thresholds
+};
+
+// One wall law (pyrdsim.pyx:1132-1145; 9-3 wall extension).
+struct WallLaw {
+  int law, type, dim, pad;
+  float c0, c1, c2, c3;
+  float rc_lo, rc_hi;             // 9-3 wall: guard band around rc (length units)
+  double r0, rc;
+  long long hr0;                  // high-word fixed value of r0 (tanh wall)
+};
+
+// One reaction (pyrdsim.pyx:2070-2223).
+struct RxDev {
+  int kind, reactant, product, catalyst, inh, inh2, pad0, pad1;
+  double rate, r0, dec;
+  float r02_lo, r02_hi;           // guard band around r0^2
+};
+
+struct TermDev {                  // bonded term; angles in radians
+  int kind, i, j, k;
+  float p0, k0, thr, pad;
+};
+
+struct TmplDev {
+  int n_atoms, n_terms, term0, atom0;  // atom0: offset into atom-term CSR
+  uint32_t bondmask[MAXA];        // bit b of [a]: (a,b) is a bonded-list pair
+};
+
+struct SysDev {
+  int p0, n;                      // particle range in the sorted arrays
+  int c0;                         // first global cell
+  int ntile0, ntiles;
+  int nc[3];                      // cells per dimension
+  int halo[3];                    // 1, or 0 where nc == 1 and periodic
+  int ntypes;
+  int periodic;                   // bit k set: dimension k periodic
+  int nlaws, nwalls, nrx;
+  int law0, wall0, rx0;
+  int angle_is_pi;
+  int has_terms;
+  int rx_any_mask;                // types that are reactant of any reaction
+  int rx_nb_mask;                 // ... of a neighbour-dependent reaction
+  double L[3];
+  double unit_d[3];               // length per fixed unit
+  double S[3];                    // reflecting: fixed value of L (as double)
+  long long Si[3];                // reflecting: fixed value of L
+  float unit_hi[3];               // length per high-word unit
+  float inv_unit_hi[3];
+  float delta;                    // allowed displacement per dimension since
+                                  // the last rebuild (length units)
+  unsigned long long hrange[3];   // high-word range used for cell mapping
+  float R2;                       // candidate radius^2 (forces + reactions)
+  float Rrx2;                     // reaction radius^2 (guarded)
+  double dt;
+  unsigned long long seed;
+  float fp[MAXT], npf[MAXT];      // dt*D and sqrt(2 dt D) per type
+  unsigned int partner[MAXT];     // bit j of [i]: types i, j are partners
+  unsigned short ppair[MAXT * MAXT];  // first law << 5 | count, symmetric
+};
+
+struct Tile {
+  int sys;
+  int c[3];
+  int w[3];
+  int pad;
+};
+
+struct ErrDev {
+  int code, dim;
+  long long particle, step;
+  double value;
+};
+
+// Kernel arguments shared by the tile kernels (passed by value).
+struct Args {
+  const SysDev* sys;
+  const Tile* tiles;
+  const PairLaw* laws;
+  const WallLaw* walls;
+  const RxDev* rx;
+  const TmplDev* tmpl;
+  const TermDev* terms;
+  const int* atomterm;            // term index * 4 + role, per template atom
+  const int* cell_start;
+  const uint32_t* xh[3];
+  const uint32_t* xl[3];
+  const uint32_t* meta;
+  const int* mol;
+  const int* pid;
+  const int* slot_of;             // caller index -> sorted slot
+  const uint32_t* xr[3];          // high words at the last rebuild
+  uint32_t* xh_out[3];
+  uint32_t* xl_out[3];
+  uint32_t* meta_out;
+  float* drift[3];
+  double* rates_out;              // reaction-rate hook (sorted order)
+  ErrDev* err;
+  const double* xi;               // injected normals for the EM step
+  const double* u1;               // injected uniforms for this step
+  const double* u2;
+  long long step;                 // step number of this kernel's work
+  long long em_step;              // step number of the fused EM update
+  int ntiles;
+  int cap;                        // staged-particle capacity (smem)
+  int n_total;
+  int flags;
+};
+
+enum : int {
+  F_STORE_DRIFT = 1,              // write the drift (sorted order)
+  F_EM = 2,                       // fuse the Euler-Maruyama update
+  F_NO_NOISE = 4,                 // random_force = False
+  F_INJECT = 8,                   // xi / u1 / u2 come from buffers
+  F_RATES_ONLY = 16,              // reaction kernel: write total rates, no draw
+  F_CHECK_SKIN = 32
+};
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
+struct U4 {
+  uint32_t x, y, z, w;
+};
+
+__host__ __device__ inline U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint64_t p0 = (uint64_t)M0 * c.x;
+    uint64_t p1 = (uint64_t)M1 * c.z;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    U4 n;
+    n.x = hi1 ^ c.y ^ k0;
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ k1;
+    n.w = lo0;
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+
+// Noise streams: tag 0 = Gaussian increments, tag 1 = reaction uniforms,
+// tag 2 = second Gaussian block (3D).
+__host__ __device__ inline U4 noise_words(unsigned long long seed, long long step,
+                                          int pid, uint32_t tag) {
+  U4 c{(uint32_t)step, (uint32_t)((unsigned long long)step >> 32), (uint32_t)pid, tag};
+  return philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+}  // namespace rd

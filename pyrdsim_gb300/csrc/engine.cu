@@ -1,0 +1,1313 @@
+// engine.cu -- host side of the GB300 step engine: the C ABI of rdsim.h.
+//
+// One handle = one CUDA stream + device buffers for a batch of independent
+// systems.  Set-up builds the flat tables (pair laws, walls, reactions,
+// bonded templates) and the tile decomposition; each rdsim_step launches,
+// per step: [EM] -> [rebuild every freq steps] -> [reactions] -> drift
+// (with the next step's EM fused in).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/rdsim.h"
+#include "device.cuh"
+#include "kernels.cuh"
+
+using namespace rd;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(RDSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr double TWO32 = 4294967296.0;
+constexpr double TWO64 = 18446744073709551616.0;
+const long long S_REFLECT = (long long)((1ULL << 63) - (1ULL << 34));
+
+struct HostSys {
+  int p0, n, pid0;
+  double cl_ref[3];
+  double rs;
+  int freq;
+  double L[3];
+  int periodic_mask;
+  long long Si[3];
+};
+
+template <class T>
+int dalloc(T** p, size_t n, int64_t* acc) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(RDSIM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  *acc += (int64_t)(n * sizeof(T));
+  return 0;
+}
+
+}  // namespace
+
+struct rdsim_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int D = 2, nsys = 0, N = 0;
+  int tpp = 4, cap = 1024;
+  size_t dyn_smem = 0;
+  int64_t step = 0;
+  int freq = 10;
+  bool has_rx = false;
+  double skin = 0, cell_min = 0, range = 0;
+  int64_t device_bytes = 0;
+  std::vector<HostSys> hs;
+  std::vector<SysDev> sys_h;
+  std::vector<Tile> tiles_h;
+  SysDev* sys_d = nullptr;
+  Tile* tiles_d = nullptr;
+  PairLaw* laws_d = nullptr;
+  WallLaw* walls_d = nullptr;
+  RxDev* rx_d = nullptr;
+  TmplDev* tmpl_d = nullptr;
+  TermDev* terms_d = nullptr;
+  int* atomterm_d = nullptr;
+  int ncells = 0, nscan = 0;
+  int *cell_count = nullptr, *cell_start = nullptr, *bsum = nullptr;
+  int *cell_of = nullptr, *rank_of = nullptr, *tmp = nullptr, *sid = nullptr, *slot_of = nullptr;
+  uint32_t* xh[2][3] = {};
+  uint32_t* xl[2][3] = {};
+  uint32_t* xr[3] = {};
+  uint32_t* meta[2] = {};
+  int* mol[2] = {};
+  int* pid[2] = {};
+  float* drift[3] = {};
+  double* rates = nullptr;
+  double* xbuf = nullptr;  // float64 positions in caller order (hooks)
+  int* tbuf = nullptr;
+  ErrDev* err = nullptr;
+  double* cl_d = nullptr;
+  int cx = 0, cm = 0, co = 0;
+  // host copies of static per-particle data (caller order)
+  std::vector<uint32_t> meta_static;  // local << 16 | template << 24
+  std::vector<int> mol_h;
+  // injected noise staging
+  double *inj_xi = nullptr, *inj_u1 = nullptr, *inj_u2 = nullptr;
+  size_t inj_steps = 0;
+  // trajectory ring
+  int traj_stride = 0, traj_frames = 0;
+  double* traj_x = nullptr;
+  int* traj_t = nullptr;
+  // kernel accounting
+  int64_t nlaunch[RDSIM_PROFILE_CLASSES] = {};
+  bool prof = false;
+  struct Pend {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pend> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  double prof_ms[RDSIM_PROFILE_CLASSES] = {};
+  int64_t prof_n[RDSIM_PROFILE_CLASSES] = {};
+};
+
+namespace {
+
+enum { P_FORCE = 0, P_REACT = 1, P_EM = 2, P_REBUILD = 3, P_HOOK = 4 };
+
+cudaEvent_t take_event(rdsim_handle* h) {
+  if (!h->ev_pool.empty()) {
+    cudaEvent_t e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Brackets the launches of one class with events when profiling is on.
+struct ProfScope {
+  rdsim_handle* h;
+  int cls;
+  cudaEvent_t a = nullptr;
+  ProfScope(rdsim_handle* h_, int c, int nkernels) : h(h_), cls(c) {
+    h->nlaunch[c] += nkernels;
+    if (h->prof) {
+      a = take_event(h);
+      cudaEventRecord(a, h->stream);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEvent_t b = take_event(h);
+      cudaEventRecord(b, h->stream);
+      h->pending.push_back({cls, a, b});
+    }
+  }
+};
+
+void resolve_profile(rdsim_handle* h) {
+  for (auto& p : h->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      h->prof_ms[p.cls] += ms;
+      h->prof_n[p.cls] += 1;
+    }
+    h->ev_pool.push_back(p.a);
+    h->ev_pool.push_back(p.b);
+  }
+  h->pending.clear();
+}
+
+Args make_args(rdsim_handle* h) {
+  Args a;
+  std::memset(&a, 0, sizeof a);
+  a.sys = h->sys_d;
+  a.tiles = h->tiles_d;
+  a.laws = h->laws_d;
+  a.walls = h->walls_d;
+  a.rx = h->rx_d;
+  a.tmpl = h->tmpl_d;
+  a.terms = h->terms_d;
+  a.atomterm = h->atomterm_d;
+  a.cell_start = h->cell_start;
+  for (int k = 0; k < 3; k++) {
+    a.xh[k] = h->xh[h->cx][k];
+    a.xl[k] = h->xl[h->cx][k];
+    a.xh_out[k] = h->xh[1 - h->cx][k];
+    a.xl_out[k] = h->xl[1 - h->cx][k];
+    a.xr[k] = h->xr[k];
+    a.drift[k] = h->drift[k];
+  }
+  a.meta = h->meta[h->cm];
+  a.meta_out = h->meta[1 - h->cm];
+  a.mol = h->mol[h->co];
+  a.pid = h->pid[h->co];
+  a.slot_of = h->slot_of;
+  a.rates_out = h->rates;
+  a.err = h->err;
+  a.ntiles = (int)h->tiles_h.size();
+  a.cap = h->cap;
+  a.n_total = h->N;
+  return a;
+}
+
+template <int D, int TPP>
+void set_smem_attrs(size_t dyn) {
+  cudaFuncSetAttribute(k_force<D, TPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  cudaFuncSetAttribute(k_react<D, TPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
+
+template <int D>
+int set_attrs_d(int tpp, size_t dyn) {
+  switch (tpp) {
+    case 1: set_smem_attrs<D, 1>(dyn); break;
+    case 2: set_smem_attrs<D, 2>(dyn); break;
+    case 4: set_smem_attrs<D, 4>(dyn); break;
+    case 8: set_smem_attrs<D, 8>(dyn); break;
+    default: return fail(RDSIM_ERR_ARG, "threads_per_particle must be 1, 2, 4 or 8");
+  }
+  return 0;
+}
+
+template <int D, int TPP>
+void launch_tile(rdsim_handle* h, bool react, const Args& a) {
+  dim3 grid((unsigned)h->tiles_h.size());
+  if (react) k_react<D, TPP><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+  else k_force<D, TPP><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+}
+
+template <int D>
+void launch_tile_d(rdsim_handle* h, bool react, const Args& a) {
+  switch (h->tpp) {
+    case 1: launch_tile<D, 1>(h, react, a); break;
+    case 2: launch_tile<D, 2>(h, react, a); break;
+    case 4: launch_tile<D, 4>(h, react, a); break;
+    default: launch_tile<D, 8>(h, react, a); break;
+  }
+}
+
+void launch_tiles(rdsim_handle* h, bool react, const Args& a) {
+  if (h->tiles_h.empty()) return;
+  if (h->D == 2) launch_tile_d<2>(h, react, a);
+  else if (h->D == 3) launch_tile_d<3>(h, react, a);
+  else launch_tile_d<1>(h, react, a);
+}
+
+unsigned nblk(int n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+int rebuild(rdsim_handle* h) {
+  const int n = h->N;
+  ProfScope ps(h, P_REBUILD, 5);
+  CK(cudaMemsetAsync(h->cell_count, 0, sizeof(int) * (size_t)h->ncells, h->stream));
+  uint32_t* const* x = h->xh[h->cx];
+  if (h->D == 2)
+    k_bin<2><<<nblk(n), 256, 0, h->stream>>>(h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+  else if (h->D == 3)
+    k_bin<3><<<nblk(n), 256, 0, h->stream>>>(h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+  else
+    k_bin<1><<<nblk(n), 256, 0, h->stream>>>(h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+  k_scan_partial<<<h->nscan, 256, 0, h->stream>>>(h->cell_count, h->ncells, h->bsum);
+  k_scan_final<<<h->nscan, 256, 0, h->stream>>>(h->cell_count, h->ncells, h->bsum, h->cell_start);
+  k_scatter<<<nblk(n), 256, 0, h->stream>>>(h->cell_of, h->rank_of, h->cell_start, n, h->tmp);
+  Args a = make_args(h);
+  OrderOut o;
+  o.mol = h->mol[1 - h->co];
+  o.pid = h->pid[1 - h->co];
+  for (int k = 0; k < 3; k++) o.xr[k] = h->xr[k];
+  o.slot_of = h->slot_of;
+  if (h->D == 2) k_order<2><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
+  else if (h->D == 3) k_order<3><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
+  else k_order<1><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
+  h->cx = 1 - h->cx;
+  h->cm = 1 - h->cm;
+  h->co = 1 - h->co;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int force(rdsim_handle* h, long long step, int flags, const double* xi_next) {
+  Args a = make_args(h);
+  a.step = step;
+  a.em_step = step + 1;
+  a.flags = flags | F_CHECK_SKIN;
+  a.xi = xi_next;
+  {
+    ProfScope ps(h, P_FORCE, 1);
+    launch_tiles(h, false, a);
+  }
+  CK(cudaGetLastError());
+  if (flags & F_EM) h->cx = 1 - h->cx;
+  return 0;
+}
+
+int react(rdsim_handle* h, long long step, int flags, const double* u1, const double* u2) {
+  Args a = make_args(h);
+  a.step = step;
+  a.flags = flags;
+  a.u1 = u1;
+  a.u2 = u2;
+  {
+    ProfScope ps(h, (flags & F_RATES_ONLY) ? P_HOOK : P_REACT, 1);
+    launch_tiles(h, true, a);
+  }
+  CK(cudaGetLastError());
+  if (!(flags & F_RATES_ONLY)) h->cm = 1 - h->cm;
+  return 0;
+}
+
+int em(rdsim_handle* h, long long step, int flags, const double* xi) {
+  Args a = make_args(h);
+  a.em_step = step;
+  a.flags = flags;
+  a.xi = xi;
+  unsigned g = nblk(h->N);
+  ProfScope ps(h, P_EM, 1);
+  if (h->D == 2) k_em<2><<<g, 256, 0, h->stream>>>(a, h->sid);
+  else if (h->D == 3) k_em<3><<<g, 256, 0, h->stream>>>(a, h->sid);
+  else k_em<1><<<g, 256, 0, h->stream>>>(a, h->sid);
+  CK(cudaGetLastError());
+  h->cx = 1 - h->cx;
+  return 0;
+}
+
+int snapshot(rdsim_handle* h, double* fx, int* ft) {
+  Args a = make_args(h);
+  unsigned g = nblk(h->N);
+  if (h->D == 2) k_snapshot<2><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, fx, ft);
+  else if (h->D == 3) k_snapshot<3><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, fx, ft);
+  else k_snapshot<1><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, fx, ft);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int check_device_error(rdsim_handle* h) {
+  ErrDev e;
+  CK(cudaMemcpyAsync(&e, h->err, sizeof e, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (e.code == 0) return 0;
+  CK(cudaMemsetAsync(h->err, 0, sizeof(ErrDev), h->stream));
+  char buf[256];
+  if (e.code == RDSIM_ERR_OUT_OF_BOUNDS) {
+    snprintf(buf, sizeof buf,
+             "x[%lld,%d] = %.17g out of bounds. Maybe the timestep is too large for the "
+             "given the interaction parameters?", e.particle, e.dim, e.value);
+  } else if (e.code == RDSIM_ERR_SKIN) {
+    snprintf(buf, sizeof buf,
+             "particle %lld moved %.6g along dimension %d since the last neighbour-list "
+             "rebuild (step %lld), more than the skin allows; increase gpu_skin or "
+             "rebuild more often", e.particle, e.value, e.dim, e.step);
+  } else if (e.code == RDSIM_ERR_NONFINITE) {
+    snprintf(buf, sizeof buf,
+             "non-finite or larger-than-box update of particle %lld, dimension %d "
+             "(value %.6g) at step %lld", e.particle, e.dim, e.value, e.step);
+  } else {
+    snprintf(buf, sizeof buf, "device error %d at step %lld", e.code, e.step);
+  }
+  return fail(e.code, buf);
+}
+
+// float64 -> 64-bit fixed point (host, long double).
+uint64_t to_fixed(double x, double L, bool periodic, long long Si) {
+  if (periodic) {
+    long double f = std::fmod((long double)x, (long double)L);
+    if (f < 0) f += (long double)L;
+    long double v = f / (long double)L * (long double)TWO64;
+    if (v >= (long double)TWO64) v -= (long double)TWO64;
+    if (v < 0) v = 0;
+    long double fl = std::floor(v + 0.5L);
+    if (fl >= (long double)TWO64) fl -= (long double)TWO64;
+    return (uint64_t)fl;
+  }
+  long double v = (long double)x / (long double)L * (long double)Si;
+  long long q = (long long)std::llround(v);
+  return (uint64_t)q;
+}
+
+int upload_state(rdsim_handle* h, const std::vector<double>& x, const std::vector<int>& types) {
+  const int N = h->N, D = h->D;
+  std::vector<uint32_t> hx[3], lx[3];
+  for (int k = 0; k < D; k++) {
+    hx[k].resize(N);
+    lx[k].resize(N);
+  }
+  std::vector<uint32_t> meta(N);
+  std::vector<int> pid(N);
+  for (int s = 0; s < h->nsys; s++) {
+    const HostSys& q = h->hs[s];
+    for (int i = 0; i < q.n; i++) {
+      const int g = q.p0 + i;  // initial slot = caller index
+      for (int k = 0; k < D; k++) {
+        double v = x[(size_t)g * D + k];
+        bool per = (q.periodic_mask >> k) & 1;
+        if (!per) {
+          if (!(v >= -q.L[k] && v <= 1.999 * q.L[k]))
+            return fail(RDSIM_ERR_ARG, "initial position outside the reflecting box");
+        } else if (!std::isfinite(v)) {
+          return fail(RDSIM_ERR_ARG, "non-finite initial position");
+        }
+        uint64_t X = to_fixed(v, q.L[k], per, q.Si[k]);
+        hx[k][g] = (uint32_t)(X >> 32);
+        lx[k][g] = (uint32_t)X;
+      }
+      int t = types[g];
+      if (t < 0 || t >= h->sys_h[s].ntypes)
+        return fail(RDSIM_ERR_ARG, "particle type without tau_by_tauD entry");
+      meta[g] = h->meta_static[g] | (uint32_t)t | ((uint32_t)t << 8);
+      pid[g] = g;
+    }
+  }
+  h->cx = h->cm = h->co = 0;
+  for (int k = 0; k < D; k++) {
+    CK(cudaMemcpyAsync(h->xh[0][k], hx[k].data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->xl[0][k], lx[k].data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  }
+  CK(cudaMemcpyAsync(h->meta[0], meta.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->mol[0], h->mol_h.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->pid[0], pid.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int initial_drift(rdsim_handle* h) {
+  int rc = rebuild(h);
+  if (rc) return rc;
+  rc = force(h, h->step, F_STORE_DRIFT, nullptr);
+  if (rc) return rc;
+  return check_device_error(h);
+}
+
+void free_all(rdsim_handle* h) {
+  auto F = [](void* p) {
+    if (p) cudaFree(p);
+  };
+  F(h->sys_d); F(h->tiles_d); F(h->laws_d); F(h->walls_d); F(h->rx_d); F(h->tmpl_d);
+  F(h->terms_d); F(h->atomterm_d); F(h->cell_count); F(h->cell_start); F(h->bsum);
+  F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
+  for (int b = 0; b < 2; b++) {
+    for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); }
+    F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
+  }
+  for (int k = 0; k < 3; k++) { F(h->xr[k]); F(h->drift[k]); }
+  F(h->rates); F(h->xbuf); F(h->tbuf); F(h->err); F(h->cl_d);
+  F(h->inj_xi); F(h->inj_u1); F(h->inj_u2); F(h->traj_x); F(h->traj_t);
+  for (auto& p : h->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (auto e : h->ev_pool) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+float guard2(double r, double unit) {  // half-width of the r^2 guard band
+  return (float)(r * r * 1e-5 + 2.0 * r * 4.0 * unit + 1e-12);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rdsim_last_error(void) { return g_err.c_str(); }
+
+int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_options* options,
+                 rdsim_handle** out) {
+  if (!systems || n_systems <= 0 || !out) return fail(RDSIM_ERR_ARG, "no systems");
+  rdsim_options opt;
+  std::memset(&opt, 0, sizeof opt);
+  if (options) opt = *options;
+  auto* h = new rdsim_handle();
+  h->device = opt.device;
+  h->D = systems[0].n_dim;
+  h->nsys = n_systems;
+  h->tpp = opt.threads_per_particle > 0 ? opt.threads_per_particle : 4;
+  if (h->tpp != 1 && h->tpp != 2 && h->tpp != 4 && h->tpp != 8) {
+    delete h;
+    return fail(RDSIM_ERR_ARG, "threads_per_particle must be 1, 2, 4 or 8");
+  }
+  int rc = 0;
+  auto bail = [&](int code) {
+    free_all(h);
+    delete h;
+    return code;
+  };
+  if (cudaSetDevice(h->device) != cudaSuccess) return bail(fail(RDSIM_ERR_CUDA, "cudaSetDevice failed"));
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(RDSIM_ERR_CUDA, "cudaStreamCreate failed"));
+  const int D = h->D;
+  if (D < 1 || D > 3) return bail(fail(RDSIM_ERR_ARG, "n_dim must be 1, 2 or 3"));
+
+  std::vector<PairLaw> laws;
+  std::vector<WallLaw> walls;
+  std::vector<RxDev> rxs;
+  std::vector<TmplDev> tmpls;
+  std::vector<TermDev> terms;
+  std::vector<int> atomterm;
+  std::vector<double> x_all;
+  std::vector<int> t_all;
+  std::vector<int> sid_h;
+  int total_cells = 0;
+  double skin_report = 0, cell_report = 1e300, range_report = 0;
+  int target = opt.tile_target > 0 ? opt.tile_target : 96;
+
+  for (int si = 0; si < n_systems; si++) {
+    const rdsim_system& S = systems[si];
+    if (S.n_dim != D) return bail(fail(RDSIM_ERR_ARG, "all systems of a batch must share n_dim"));
+    if (S.n_particles <= 0) return bail(fail(RDSIM_ERR_ARG, "system without particles"));
+    if (S.n_types <= 0 || S.n_types > MAXT) return bail(fail(RDSIM_ERR_UNSUPPORTED, "1..16 particle types supported"));
+    if (S.n_interactions > MAXI) return bail(fail(RDSIM_ERR_UNSUPPORTED, "at most 32 interactions per system"));
+    if (S.n_reactions > MAXR) return bail(fail(RDSIM_ERR_UNSUPPORTED, "at most 8 reactions per system"));
+    if (S.neighbor_list_update_frequency <= 0) return bail(fail(RDSIM_ERR_ARG, "neighbor_list_update_frequency must be positive"));
+    if (si == 0) h->freq = S.neighbor_list_update_frequency;
+    else if (S.neighbor_list_update_frequency != h->freq)
+      return bail(fail(RDSIM_ERR_UNSUPPORTED, "batched systems must share neighbor_list_update_frequency"));
+    SysDev sd;
+    std::memset(&sd, 0, sizeof sd);
+    HostSys hsys;
+    std::memset(&hsys, 0, sizeof hsys);
+    sd.p0 = h->N;
+    sd.n = S.n_particles;
+    sd.ntypes = S.n_types;
+    sd.dt = S.dt;
+    sd.seed = S.seed ^ (0x9E3779B97F4A7C15ULL * (unsigned long long)si);
+    sd.angle_is_pi = S.angle_is_pi;
+    hsys.p0 = h->N;
+    hsys.n = S.n_particles;
+    hsys.pid0 = h->N;
+    hsys.rs = S.rs;
+    hsys.freq = S.neighbor_list_update_frequency;
+    double max_unit = 0;
+    for (int k = 0; k < D; k++) {
+      if (!(S.L[k] > 0)) return bail(fail(RDSIM_ERR_ARG, "box lengths must be positive"));
+      sd.L[k] = S.L[k];
+      hsys.L[k] = S.L[k];
+      // pyrdsim.pyx:2266 wraps for periodic >= 0 but applies the minimum image
+      // only for periodic > 0 (1540-1564, 1629); the mixed case 0 is rejected
+      if (S.periodic[k] == 0)
+        return bail(fail(RDSIM_ERR_UNSUPPORTED, "periodic must be > 0 (periodic) or < 0 (reflecting)"));
+      const bool per = S.periodic[k] > 0;
+      if (per) {
+        sd.periodic |= 1 << k;
+        hsys.periodic_mask |= 1 << k;
+        sd.unit_d[k] = S.L[k] / TWO64;
+        sd.unit_hi[k] = (float)(S.L[k] / TWO32);
+        sd.inv_unit_hi[k] = (float)(TWO32 / S.L[k]);
+        sd.hrange[k] = 1ULL << 32;
+      } else {
+        sd.Si[k] = S_REFLECT;
+        hsys.Si[k] = S_REFLECT;
+        sd.S[k] = (double)S_REFLECT;
+        sd.unit_d[k] = S.L[k] / (double)S_REFLECT;
+        sd.unit_hi[k] = (float)(S.L[k] * TWO32 / (double)S_REFLECT);
+        sd.inv_unit_hi[k] = (float)((double)S_REFLECT / (S.L[k] * TWO32));
+        sd.hrange[k] = ((unsigned long long)S_REFLECT >> 32) + 1;
+      }
+      max_unit = std::max(max_unit, (double)sd.unit_hi[k]);
+    }
+    // reference cell geometry for the cell-id hook (pyrdsim.pyx:1436-1444)
+    if (S.rs > 0 && S.cell_length_ratio > 0) {
+      for (int k = 0; k < D; k++) {
+        int l = 1;
+        while (S.L[k] / (double)(l + 1) >= S.rs / (double)S.cell_length_ratio && l < (1 << 28)) l += 1;
+        hsys.cl_ref[k] = S.L[k] / (double)l;
+      }
+    }
+    // per-type prefactors (pyrdsim.pyx:488-496) and partners (1157-1263)
+    for (int t = 0; t < S.n_types; t++) {
+      double tau = S.tau_by_tauD[t];
+      if (tau < 0) {
+        sd.fp[t] = 0.f;
+        sd.npf[t] = 0.f;
+      } else {
+        sd.fp[t] = (float)(S.dt * tau);
+        sd.npf[t] = (float)std::sqrt(2.0 * S.dt * tau);
+      }
+    }
+    auto add_partner = [&](int a, int b) -> bool {
+      if (a < 0 || b < 0 || a >= MAXT || b >= MAXT) return false;
+      sd.partner[a] |= 1u << b;
+      sd.partner[b] |= 1u << a;
+      return true;
+    };
+    // pair laws grouped by sorted type pair, file order within a pair
+    sd.law0 = (int)laws.size();
+    sd.wall0 = (int)walls.size();
+    double R = 0;
+    std::vector<std::vector<PairLaw>> by_pair(MAXT * MAXT);
+    for (int q = 0; q < S.n_interactions; q++) {
+      const rdsim_interaction& it = S.interactions[q];
+      if (it.law == RDSIM_LAW_WALL || it.law == RDSIM_LAW_WALL93) {
+        if (it.type_b < 0 || it.type_b >= D) return bail(fail(RDSIM_ERR_ARG, "wall direction out of range"));
+        if ((int)walls.size() - sd.wall0 >= MAXW) return bail(fail(RDSIM_ERR_UNSUPPORTED, "at most 8 walls per system"));
+        WallLaw w;
+        std::memset(&w, 0, sizeof w);
+        w.law = it.law;
+        w.type = it.type_a;
+        w.dim = it.type_b;
+        w.r0 = it.r0;
+        w.rc = it.rc;
+        if (it.law == RDSIM_LAW_WALL) {
+          if (it.a == 0) return bail(fail(RDSIM_ERR_ARG, "wall with a = 0"));
+          w.c0 = (float)(it.u0 * (1.0 / it.a) / 2.0);
+          w.c2 = (float)(1.0 / it.a);
+          w.hr0 = (long long)std::llround(it.r0 / (double)sd.unit_hi[w.dim]);
+        } else {
+          w.c0 = (float)it.u0;
+          w.c1 = (float)it.r0;
+          w.rc_lo = (float)(it.rc * (1 - 1e-5) - 4 * sd.unit_hi[w.dim]);
+          w.rc_hi = (float)(it.rc * (1 + 1e-5) + 4 * sd.unit_hi[w.dim]);
+        }
+        walls.push_back(w);
+        continue;
+      }
+      if (it.law < RDSIM_LAW_LJ || it.law > RDSIM_LAW_PIECEWISE_LINEAR)
+        return bail(fail(RDSIM_ERR_ARG, "unknown interaction law"));
+      if (!add_partner(it.type_a, it.type_b)) return bail(fail(RDSIM_ERR_UNSUPPORTED, "interaction type out of range"));
+      // pyrdsim.pyx:1999-2007: only a pair listed as (small, large) ever matches
+      if (it.type_a > it.type_b) continue;
+      PairLaw L;
+      std::memset(&L, 0, sizeof L);
+      L.law = it.law;
+      L.n = it.n;
+      double rc = it.law == RDSIM_LAW_PIECEWISE_LINEAR ? it.r0 : it.rc;
+      L.rc = rc;
+      switch (it.law) {
+        case RDSIM_LAW_LJ:
+          L.c0 = (float)(-2.0 * it.n * it.u0);
+          L.c1 = (float)(it.r0 * it.r0);
+          break;
+        case RDSIM_LAW_TANH:
+          if (it.a == 0) return bail(fail(RDSIM_ERR_ARG, "tanh interaction with a = 0"));
+          L.c0 = (float)(it.u0 * (1.0 / it.a) / 2.0);
+          L.c1 = (float)it.r0;
+          L.c2 = (float)(1.0 / it.a);
+          break;
+        case RDSIM_LAW_YUKAWA:
+          L.c0 = (float)(-it.u0 / it.r0);
+          L.c1 = (float)it.r0;
+          L.c2 = (float)(1.0 / it.r0);
+          break;
+        case RDSIM_LAW_HARMONIC:
+          L.c0 = (float)it.u0;
+          break;
+        case RDSIM_LAW_PIECEWISE_LINEAR:
+          L.c0 = (float)(it.u0 / it.dr);
+          L.rin = it.r0 - it.dr;
+          break;
+      }
+      float g = guard2(rc, max_unit);
+      L.rc2_lo = (float)(rc * rc) - g;
+      L.rc2_hi = (float)(rc * rc) + g;
+      if (it.law == RDSIM_LAW_PIECEWISE_LINEAR) {
+        double ri = std::max(0.0, L.rin);
+        float gi2 = guard2(ri, max_unit);
+        L.in2_lo = (float)(ri * ri) - gi2;
+        L.in2_hi = (float)(ri * ri) + gi2;
+      }
+      if (rc > 0) R = std::max(R, rc);
+      by_pair[it.type_a * MAXT + it.type_b].push_back(L);
+    }
+    float R2 = 0.f;
+    for (int a = 0; a < MAXT; a++)
+      for (int b = a; b < MAXT; b++) {
+        auto& v = by_pair[a * MAXT + b];
+        if (v.empty()) continue;
+        int first = (int)laws.size() - sd.law0;
+        if (first + (int)v.size() > 2047) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many pair laws"));
+        for (auto& L : v) {
+          laws.push_back(L);
+          R2 = std::max(R2, L.rc2_hi);
+        }
+        unsigned short code = (unsigned short)((first << 5) | (int)v.size());
+        sd.ppair[a * MAXT + b] = code;
+        sd.ppair[b * MAXT + a] = code;
+      }
+    sd.nlaws = (int)laws.size() - sd.law0;
+    sd.nwalls = (int)walls.size() - sd.wall0;
+    if (sd.nlaws > MAXI) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many pair laws"));
+    // reactions
+    sd.rx0 = (int)rxs.size();
+    float Rrx2 = 0.f;
+    for (int q = 0; q < S.n_reactions; q++) {
+      const rdsim_reaction& r = S.reactions[q];
+      RxDev x;
+      std::memset(&x, 0, sizeof x);
+      x.kind = r.kind;
+      x.reactant = r.reactant;
+      x.product = r.product;
+      x.catalyst = r.catalyst;
+      x.inh = r.inhibitor;
+      x.inh2 = r.inhibitor2;
+      x.rate = r.rate;
+      x.r0 = r.r0;
+      x.dec = r.rate_decrease;
+      if (r.product < 0 || r.product >= S.n_types || r.reactant < 0 || r.reactant >= MAXT)
+        return bail(fail(RDSIM_ERR_UNSUPPORTED, "reaction types out of range"));
+      if (r.kind != RDSIM_RX_LINEAR) {
+        if (r.kind == RDSIM_RX_CATALYZED) {
+          if (!add_partner(r.reactant, r.catalyst)) return bail(fail(RDSIM_ERR_UNSUPPORTED, "reaction type out of range"));
+        } else if (r.kind == RDSIM_RX_INHIBITED) {
+          if (!add_partner(r.reactant, r.inhibitor)) return bail(fail(RDSIM_ERR_UNSUPPORTED, "reaction type out of range"));
+          if (r.inhibitor2 >= 0) add_partner(r.reactant, r.inhibitor2);
+        } else {
+          return bail(fail(RDSIM_ERR_ARG, "unknown reaction kind"));
+        }
+        float g = guard2(r.r0, max_unit);
+        x.r02_lo = (float)(r.r0 * r.r0) - g;
+        x.r02_hi = (float)(r.r0 * r.r0) + g;
+        Rrx2 = std::max(Rrx2, x.r02_hi);
+        R = std::max(R, r.r0);
+        sd.rx_nb_mask |= 1 << r.reactant;
+      }
+      sd.rx_any_mask |= 1 << r.reactant;
+      rxs.push_back(x);
+    }
+    sd.nrx = S.n_reactions;
+    if (S.n_reactions > 0) h->has_rx = true;
+    sd.R2 = R2;
+    sd.Rrx2 = Rrx2;
+    // skin: diffusion over one rebuild period plus margin, within rs
+    double sig = 0;
+    for (int t = 0; t < S.n_types; t++)
+      if (S.tau_by_tauD[t] > 0) sig = std::max(sig, std::sqrt(2.0 * S.dt * S.tau_by_tauD[t]));
+    double skin = opt.skin > 0 ? opt.skin : 10.0 * sig * std::sqrt((double)h->freq) + 0.05 * R + 0.1;
+    double delta = skin / 2;
+    if (R > 0) {
+      double room = (S.rs - R) / (2.0 * std::sqrt((double)D));
+      if (room <= 1e-6 * R)
+        return bail(fail(RDSIM_ERR_UNSUPPORTED,
+                         "rs must exceed the largest interaction / reaction range"));
+      delta = std::min(delta, room);
+    }
+    double cmin = R > 0 ? R + 2 * delta : 0;
+    skin_report = std::max(skin_report, 2 * delta);
+    range_report = std::max(range_report, R);
+    // with no pair work the displacement check is off
+    sd.delta = R > 0 ? (float)delta : 1e30f;
+    // cells
+    int ncs = 1;
+    for (int k = 0; k < D; k++) {
+      int nc;
+      if (cmin <= 0) nc = std::max(1, (int)std::min(64.0, S.L[k]));
+      else nc = (int)std::floor(S.L[k] / cmin);
+      if (nc < 1) nc = 1;
+      if ((sd.periodic >> k) & 1) {
+        if (nc < 3) nc = 1;
+      }
+      nc = std::min(nc, 1 << 16);
+      sd.nc[k] = nc;
+      sd.halo[k] = (((sd.periodic >> k) & 1) && nc == 1) ? 0 : 1;
+      if (nc == 1 && !((sd.periodic >> k) & 1)) sd.halo[k] = 0;
+      ncs *= nc;
+      cell_report = std::min(cell_report, S.L[k] / nc);
+    }
+    sd.c0 = total_cells;
+    total_cells += ncs;
+    if (total_cells < 0 || total_cells > (1 << 28)) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many cells"));
+    // tiles
+    double per_cell = (double)S.n_particles / ncs;
+    double cells_per_tile = std::max(1.0, target / std::max(per_cell, 1e-9));
+    int w[3] = {1, 1, 1};
+    double side = std::pow(cells_per_tile, 1.0 / D);
+    for (int k = 0; k < D; k++) {
+      int wk = std::max(1, (int)std::lround(side));
+      int lim = sd.nc[k];
+      if (((sd.periodic >> k) & 1) && sd.nc[k] >= 3) lim = sd.nc[k] - 2;
+      if (sd.nc[k] == 1) lim = 1;
+      wk = std::min(wk, lim);
+      w[k] = wk;
+    }
+    auto halo_cells = [&]() {
+      int p = 1;
+      for (int k = 0; k < D; k++) p *= w[k] + 2 * sd.halo[k];
+      return p;
+    };
+    while (halo_cells() > MAXHC) {
+      int kk = 0;
+      for (int k = 1; k < D; k++)
+        if (w[k] > w[kk]) kk = k;
+      if (w[kk] == 1) break;
+      w[kk]--;
+    }
+    if (halo_cells() > MAXHC) return bail(fail(RDSIM_ERR_UNSUPPORTED, "tile halo too large"));
+    sd.ntile0 = (int)h->tiles_h.size();
+    int nt[3] = {1, 1, 1};
+    for (int k = 0; k < D; k++) nt[k] = (sd.nc[k] + w[k] - 1) / w[k];
+    for (int tz = 0; tz < nt[2]; tz++)
+      for (int ty = 0; ty < nt[1]; ty++)
+        for (int tx = 0; tx < nt[0]; tx++) {
+          Tile t;
+          std::memset(&t, 0, sizeof t);
+          t.sys = si;
+          int tt[3] = {tx, ty, tz};
+          for (int k = 0; k < D; k++) {
+            t.c[k] = tt[k] * w[k];
+            t.w[k] = std::min(w[k], sd.nc[k] - t.c[k]);
+          }
+          h->tiles_h.push_back(t);
+        }
+    sd.ntiles = (int)h->tiles_h.size() - sd.ntile0;
+    // bonded templates
+    std::map<int, int> tmpl_index;  // molecule_id -> device template
+    std::vector<int> tmpl_of_mol(S.n_molecules, 0xff);
+    for (int m = 0; m < S.n_molecules; m++) {
+      int j = S.first_index_of_molecule[m];
+      if (j < 0 || j >= S.n_particles) return bail(fail(RDSIM_ERR_ARG, "first_index_of_molecule out of range"));
+      int mid = S.molecule_ids[3 * j + 2];
+      int tq = -1;
+      for (int q = 0; q < S.n_templates; q++)
+        if (S.templates[q].molecule_id == mid) tq = q;
+      if (tq < 0) return bail(fail(RDSIM_ERR_ARG, "molecule id " + std::to_string(mid) + " has no definition"));
+      const rdsim_template& T = S.templates[tq];
+      if (T.n_terms == 0) continue;
+      auto it = tmpl_index.find(mid);
+      if (it == tmpl_index.end()) {
+        TmplDev td;
+        std::memset(&td, 0, sizeof td);
+        int maxatom = 0;
+        for (int e = 0; e < T.n_terms; e++) {
+          const rdsim_term& tr = S.terms[T.first_term + e];
+          maxatom = std::max(maxatom, std::max(tr.i, tr.j));
+          if (tr.kind == RDSIM_TERM_ANGLE) maxatom = std::max(maxatom, tr.k);
+          if (tr.i < 0 || tr.j < 0 || (tr.kind == RDSIM_TERM_ANGLE && tr.k < 0))
+            return bail(fail(RDSIM_ERR_ARG, "negative atom index in bonded term"));
+        }
+        if (maxatom >= MAXA) return bail(fail(RDSIM_ERR_UNSUPPORTED, "molecules with bonded terms are limited to 32 atoms"));
+        td.n_atoms = maxatom + 1;
+        td.n_terms = T.n_terms;
+        td.term0 = (int)terms.size();
+        std::vector<std::vector<int>> per_atom(td.n_atoms);
+        for (int e = 0; e < T.n_terms; e++) {
+          const rdsim_term& tr = S.terms[T.first_term + e];
+          TermDev d;
+          std::memset(&d, 0, sizeof d);
+          d.kind = tr.kind;
+          d.i = tr.i;
+          d.j = tr.j;
+          d.k = tr.k;
+          d.p0 = (float)tr.p0;
+          d.k0 = (float)tr.k0;
+          d.thr = (float)(tr.p0 - 0.1);
+          int ti = (int)terms.size();
+          terms.push_back(d);
+          per_atom[tr.i].push_back(ti * 4 + 0);
+          per_atom[tr.j].push_back(ti * 4 + 1);
+          td.bondmask[tr.i] |= 1u << tr.j;
+          td.bondmask[tr.j] |= 1u << tr.i;
+          if (tr.kind == RDSIM_TERM_ANGLE) {
+            per_atom[tr.k].push_back(ti * 4 + 2);
+            td.bondmask[tr.j] |= 1u << tr.k;
+            td.bondmask[tr.k] |= 1u << tr.j;
+          }
+        }
+        // CSR: atomterm[atom0 + a] .. atomterm[atom0 + a + 1] index the entry list
+        td.atom0 = (int)atomterm.size();
+        atomterm.resize(atomterm.size() + td.n_atoms + 1);
+        for (int a = 0; a <= td.n_atoms; a++) atomterm[td.atom0 + a] = 0;
+        int idx = (int)tmpls.size();
+        tmpls.push_back(td);
+        tmpl_index[mid] = idx;
+        // entries appended after the offsets; offsets are absolute
+        TmplDev& tt = tmpls.back();
+        for (int a = 0; a < tt.n_atoms; a++) {
+          atomterm[tt.atom0 + a] = (int)atomterm.size();
+          for (int v : per_atom[a]) atomterm.push_back(v);
+        }
+        atomterm[tt.atom0 + tt.n_atoms] = (int)atomterm.size();
+        if ((int)tmpls.size() > 0xfe) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many molecule templates"));
+        it = tmpl_index.find(mid);
+      }
+      tmpl_of_mol[m] = it->second;
+      sd.has_terms = 1;
+    }
+    // static per-particle metadata (caller order)
+    std::vector<int> mol_range_start(S.n_particles, -1), mol_of(S.n_particles, -1);
+    for (int m = 0; m < S.n_molecules; m++) {
+      int b = S.first_index_of_molecule[m];
+      int e = (m + 1 < S.n_molecules) ? S.first_index_of_molecule[m + 1] : S.n_particles;
+      for (int i = b; i < e && i < S.n_particles; i++) {
+        mol_range_start[i] = b;
+        mol_of[i] = m;
+      }
+    }
+    for (int i = 0; i < S.n_particles; i++) {
+      uint32_t ms = 0xffu << 24;
+      int m = mol_of[i];
+      if (m >= 0 && tmpl_of_mol[m] != 0xff) {
+        int loc = i - mol_range_start[i];
+        const TmplDev& td = tmpls[tmpl_of_mol[m]];
+        int msize = ((m + 1 < S.n_molecules) ? S.first_index_of_molecule[m + 1] : S.n_particles) - mol_range_start[i];
+        if (td.n_atoms > msize)
+          return bail(fail(RDSIM_ERR_UNSUPPORTED, "bonded term references an atom beyond its molecule"));
+        if (loc < td.n_atoms) ms = ((uint32_t)tmpl_of_mol[m] << 24) | ((uint32_t)loc << 16);
+      }
+      h->meta_static.push_back(ms);
+      h->mol_h.push_back(S.molecule_ids[3 * i]);
+      x_all.insert(x_all.end(), S.x + (size_t)i * D, S.x + (size_t)(i + 1) * D);
+      t_all.push_back(S.particle_types[i]);
+      sid_h.push_back(si);
+    }
+    // molecule labels must identify molecules for the same-molecule tests
+    {
+      std::map<int, int> label_mol;
+      for (int i = 0; i < S.n_particles; i++) {
+        if (mol_of[i] < 0) continue;
+        auto it = label_mol.find(S.molecule_ids[3 * i]);
+        if (it == label_mol.end()) label_mol[S.molecule_ids[3 * i]] = mol_of[i];
+        else if (it->second != mol_of[i] && tmpl_of_mol[mol_of[i]] != 0xff)
+          return bail(fail(RDSIM_ERR_UNSUPPORTED, "molecule numbers (column 0) must differ between bonded molecules"));
+      }
+    }
+    h->N += S.n_particles;
+    h->sys_h.push_back(sd);
+    h->hs.push_back(hsys);
+  }
+  h->skin = skin_report;
+  h->cell_min = cell_report;
+  h->range = range_report;
+  h->ncells = total_cells;
+  h->nscan = std::max(1, (total_cells + SCAN_TILE - 1) / SCAN_TILE);
+  // staging capacity from the expected halo population (x4 margin)
+  {
+    double worst = 0;
+    for (const SysDev& sd : h->sys_h) {
+      int ncs = 1;
+      for (int k = 0; k < D; k++) ncs *= sd.nc[k];
+      const Tile& t = h->tiles_h[sd.ntile0];
+      int hc = 1;
+      for (int k = 0; k < D; k++) hc *= t.w[k] + 2 * sd.halo[k];
+      worst = std::max(worst, 4.0 * hc * (double)sd.n / ncs);
+    }
+    int cap = (int)std::ceil(worst / 256.0) * 256;
+    h->cap = std::max(512, std::min(4096, cap));
+    h->dyn_smem = (size_t)h->cap * (D + 3) * 4;
+  }
+  // device memory
+  int64_t& B = h->device_bytes;
+  const int N = h->N;
+  if ((rc = dalloc(&h->sys_d, h->sys_h.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->tiles_d, h->tiles_h.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->laws_d, laws.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->walls_d, walls.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->rx_d, rxs.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->tmpl_d, tmpls.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->terms_d, terms.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->atomterm_d, atomterm.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->cell_count, (size_t)h->ncells, &B))) return bail(rc);
+  if ((rc = dalloc(&h->cell_start, (size_t)h->ncells + 1, &B))) return bail(rc);
+  if ((rc = dalloc(&h->bsum, (size_t)h->nscan, &B))) return bail(rc);
+  if ((rc = dalloc(&h->cell_of, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->rank_of, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->tmp, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->sid, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->slot_of, N, &B))) return bail(rc);
+  for (int b = 0; b < 2; b++) {
+    for (int k = 0; k < D; k++) {
+      if ((rc = dalloc(&h->xh[b][k], N, &B))) return bail(rc);
+      if ((rc = dalloc(&h->xl[b][k], N, &B))) return bail(rc);
+    }
+    if ((rc = dalloc(&h->meta[b], N, &B))) return bail(rc);
+    if ((rc = dalloc(&h->mol[b], N, &B))) return bail(rc);
+    if ((rc = dalloc(&h->pid[b], N, &B))) return bail(rc);
+  }
+  for (int k = 0; k < D; k++) {
+    if ((rc = dalloc(&h->xr[k], N, &B))) return bail(rc);
+    if ((rc = dalloc(&h->drift[k], N, &B))) return bail(rc);
+  }
+  if ((rc = dalloc(&h->rates, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->xbuf, (size_t)N * D, &B))) return bail(rc);
+  if ((rc = dalloc(&h->tbuf, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->err, 1, &B))) return bail(rc);
+  if ((rc = dalloc(&h->cl_d, (size_t)3 * h->nsys, &B))) return bail(rc);
+  auto up = [&](void* d, const void* s, size_t bytes) -> int {
+    if (bytes == 0) return 0;
+    CK(cudaMemcpyAsync(d, s, bytes, cudaMemcpyHostToDevice, h->stream));
+    return 0;
+  };
+  std::vector<double> cl(3 * h->nsys, 1.0);
+  for (int s = 0; s < h->nsys; s++)
+    for (int k = 0; k < D; k++) cl[3 * s + k] = h->hs[s].cl_ref[k];
+  if ((rc = up(h->sys_d, h->sys_h.data(), sizeof(SysDev) * h->sys_h.size()))) return bail(rc);
+  if ((rc = up(h->tiles_d, h->tiles_h.data(), sizeof(Tile) * h->tiles_h.size()))) return bail(rc);
+  if ((rc = up(h->laws_d, laws.data(), sizeof(PairLaw) * laws.size()))) return bail(rc);
+  if ((rc = up(h->walls_d, walls.data(), sizeof(WallLaw) * walls.size()))) return bail(rc);
+  if ((rc = up(h->rx_d, rxs.data(), sizeof(RxDev) * rxs.size()))) return bail(rc);
+  if ((rc = up(h->tmpl_d, tmpls.data(), sizeof(TmplDev) * tmpls.size()))) return bail(rc);
+  if ((rc = up(h->terms_d, terms.data(), sizeof(TermDev) * terms.size()))) return bail(rc);
+  if ((rc = up(h->atomterm_d, atomterm.data(), sizeof(int) * atomterm.size()))) return bail(rc);
+  if ((rc = up(h->sid, sid_h.data(), sizeof(int) * sid_h.size()))) return bail(rc);
+  if ((rc = up(h->cl_d, cl.data(), sizeof(double) * cl.size()))) return bail(rc);
+  if (cudaMemsetAsync(h->err, 0, sizeof(ErrDev), h->stream) != cudaSuccess)
+    return bail(fail(RDSIM_ERR_CUDA, "memset"));
+  for (int k = 0; k < D; k++)
+    if (cudaMemsetAsync(h->drift[k], 0, sizeof(float) * N, h->stream) != cudaSuccess)
+      return bail(fail(RDSIM_ERR_CUDA, "memset"));
+  if (D == 2) rc = set_attrs_d<2>(h->tpp, h->dyn_smem);
+  else if (D == 3) rc = set_attrs_d<3>(h->tpp, h->dyn_smem);
+  else rc = set_attrs_d<1>(h->tpp, h->dyn_smem);
+  if (rc) return bail(rc);
+  if ((rc = upload_state(h, x_all, t_all))) return bail(rc);
+  if ((rc = initial_drift(h))) return bail(rc);
+  *out = h;
+  return 0;
+}
+
+int rdsim_destroy(rdsim_handle* h) {
+  if (!h) return 0;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return 0;
+}
+
+int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi,
+               const double* u1, const double* u2) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  if (n_steps <= 0) return 0;
+  CK(cudaSetDevice(h->device));
+  const int N = h->N, D = h->D;
+  int kf = 0;
+  if (flags & RDSIM_STEP_NO_NOISE) kf |= F_NO_NOISE;
+  const bool inj = (flags & (RDSIM_STEP_INJECT_HOST | RDSIM_STEP_INJECT_DEVICE)) != 0;
+  const double *dxi = nullptr, *du1 = nullptr, *du2 = nullptr;
+  if (inj) {
+    kf |= F_INJECT;
+    if (flags & RDSIM_STEP_INJECT_HOST) {
+      if ((size_t)n_steps > h->inj_steps) {
+        if (h->inj_xi) cudaFree(h->inj_xi);
+        if (h->inj_u1) cudaFree(h->inj_u1);
+        if (h->inj_u2) cudaFree(h->inj_u2);
+        h->inj_xi = h->inj_u1 = h->inj_u2 = nullptr;
+        int64_t dummy = 0;
+        int rc;
+        if ((rc = dalloc(&h->inj_xi, (size_t)n_steps * N * D, &dummy))) return rc;
+        if ((rc = dalloc(&h->inj_u1, (size_t)n_steps * N, &dummy))) return rc;
+        if ((rc = dalloc(&h->inj_u2, (size_t)n_steps * N, &dummy))) return rc;
+        h->inj_steps = n_steps;
+      }
+      if (xi) CK(cudaMemcpyAsync(h->inj_xi, xi, sizeof(double) * n_steps * N * D, cudaMemcpyHostToDevice, h->stream));
+      else CK(cudaMemsetAsync(h->inj_xi, 0, sizeof(double) * n_steps * N * D, h->stream));
+      if (u1) CK(cudaMemcpyAsync(h->inj_u1, u1, sizeof(double) * n_steps * N, cudaMemcpyHostToDevice, h->stream));
+      else CK(cudaMemsetAsync(h->inj_u1, 0x7f, sizeof(double) * n_steps * N, h->stream));
+      if (u2) CK(cudaMemcpyAsync(h->inj_u2, u2, sizeof(double) * n_steps * N, cudaMemcpyHostToDevice, h->stream));
+      else CK(cudaMemsetAsync(h->inj_u2, 0x7f, sizeof(double) * n_steps * N, h->stream));
+      dxi = h->inj_xi;
+      du1 = h->inj_u1;
+      du2 = h->inj_u2;
+    } else {
+      dxi = xi;
+      du1 = u1;
+      du2 = u2;
+      if (!xi && !(flags & RDSIM_STEP_NO_NOISE)) return fail(RDSIM_ERR_ARG, "injected noise missing");
+      if (h->has_rx && (!u1 || !u2)) return fail(RDSIM_ERR_ARG, "injected uniforms missing");
+    }
+  }
+  int rc;
+  for (int q = 0; q < n_steps; q++) {
+    const long long s = h->step + 1;
+    if (q == 0) {
+      if ((rc = em(h, s, kf, dxi))) return rc;
+    }
+    if (s % h->freq == 0) {
+      if ((rc = rebuild(h))) return rc;
+    }
+    if (h->has_rx) {
+      if ((rc = react(h, s, kf, du1 ? du1 + (size_t)q * N : nullptr,
+                      du2 ? du2 + (size_t)q * N : nullptr)))
+        return rc;
+    }
+    if (h->traj_frames > 0 && s % h->traj_stride == 0) {
+      long long m = (s / h->traj_stride - 1) % h->traj_frames;
+      if ((rc = snapshot(h, h->traj_x + (size_t)m * N * D, h->traj_t + (size_t)m * N))) return rc;
+    }
+    const bool last = q == n_steps - 1;
+    const double* xn = (dxi && !last) ? dxi + (size_t)(q + 1) * N * D : nullptr;
+    if ((rc = force(h, s, last ? F_STORE_DRIFT | kf : F_EM | kf, xn))) return rc;
+    h->step = s;
+  }
+  return check_device_error(h);
+}
+
+int rdsim_set_state(rdsim_handle* h, const double* x, const int32_t* types) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  const int N = h->N, D = h->D;
+  std::vector<double> xv((size_t)N * D);
+  std::vector<int> tv(N);
+  if (!x || !types) {
+    int rc = rdsim_get_state(h, x ? nullptr : xv.data(), types ? nullptr : tv.data());
+    if (rc) return rc;
+  }
+  if (x) std::memcpy(xv.data(), x, sizeof(double) * (size_t)N * D);
+  if (types) std::memcpy(tv.data(), types, sizeof(int) * (size_t)N);
+  int rc = upload_state(h, xv, tv);
+  if (rc) return rc;
+  return initial_drift(h);
+}
+
+int rdsim_get_state(rdsim_handle* h, double* x, int32_t* types) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  Args a = make_args(h);
+  unsigned g = nblk(h->N);
+  if (h->D == 2) k_to_double<2><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, h->xbuf, h->tbuf);
+  else if (h->D == 3) k_to_double<3><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, h->xbuf, h->tbuf);
+  else k_to_double<1><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, h->xbuf, h->tbuf);
+  CK(cudaGetLastError());
+  if (x) CK(cudaMemcpyAsync(x, h->xbuf, sizeof(double) * (size_t)h->N * h->D, cudaMemcpyDeviceToHost, h->stream));
+  if (types) CK(cudaMemcpyAsync(types, h->tbuf, sizeof(int) * (size_t)h->N, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int rdsim_get_drift(rdsim_handle* h, double* a) {
+  if (!h || !a) return fail(RDSIM_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  const int N = h->N, D = h->D;
+  std::vector<float> d[3];
+  std::vector<int> pid(N);
+  for (int k = 0; k < D; k++) {
+    d[k].resize(N);
+    CK(cudaMemcpyAsync(d[k].data(), h->drift[k], 4 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(cudaMemcpyAsync(pid.data(), h->pid[h->co], 4 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < N; i++)
+    for (int k = 0; k < D; k++) a[(size_t)pid[i] * D + k] = (double)d[k][i];
+  return 0;
+}
+
+int rdsim_get_reaction_rates(rdsim_handle* h, double* total) {
+  if (!h || !total) return fail(RDSIM_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemsetAsync(h->rates, 0, sizeof(double) * h->N, h->stream));
+  if (h->has_rx) {
+    int rc = react(h, h->step, F_RATES_ONLY, nullptr, nullptr);
+    if (rc) return rc;
+  }
+  CK(cudaMemcpyAsync(total, h->rates, sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int rdsim_get_pairs(rdsim_handle* h, int32_t sys, int32_t* pairs, int64_t cap, int64_t* n_pairs) {
+  if (!h || sys < 0 || sys >= h->nsys || !n_pairs) return fail(RDSIM_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  const HostSys& q = h->hs[sys];
+  const SysDev& sd = h->sys_h[sys];
+  unsigned long long* cnt = nullptr;
+  int* buf = nullptr;
+  size_t bcap = (size_t)std::max<int64_t>(cap, 1);
+  CK(cudaMalloc(&cnt, sizeof(unsigned long long)));
+  if (cudaMalloc(&buf, sizeof(int) * 2 * bcap) != cudaSuccess) {
+    cudaFree(cnt);
+    return fail(RDSIM_ERR_NOMEM, "pair buffer");
+  }
+  cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), h->stream);
+  double maxu = 0;
+  for (int k = 0; k < h->D; k++) maxu = std::max(maxu, (double)sd.unit_hi[k]);
+  float rs2_hi = (float)(q.rs * q.rs) + guard2(q.rs, maxu);
+  Args a = make_args(h);
+  unsigned g = nblk(q.n);
+  if (h->D == 2) k_pairs<2><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, h->tmpl_d, q.rs, rs2_hi, q.p0, q.n, q.pid0, buf, (unsigned long long)cap, cnt);
+  else if (h->D == 3) k_pairs<3><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, h->tmpl_d, q.rs, rs2_hi, q.p0, q.n, q.pid0, buf, (unsigned long long)cap, cnt);
+  else k_pairs<1><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, h->tmpl_d, q.rs, rs2_hi, q.p0, q.n, q.pid0, buf, (unsigned long long)cap, cnt);
+  unsigned long long n = 0;
+  cudaError_t e1 = cudaGetLastError();
+  cudaMemcpyAsync(&n, cnt, sizeof n, cudaMemcpyDeviceToHost, h->stream);
+  cudaStreamSynchronize(h->stream);
+  *n_pairs = (int64_t)n;
+  int rc = 0;
+  if (e1 != cudaSuccess) rc = fail(RDSIM_ERR_CUDA, cudaGetErrorString(e1));
+  else if ((int64_t)n > cap) rc = fail(RDSIM_ERR_CAPACITY, "pair buffer too small");
+  else if (n > 0 && pairs) {
+    std::vector<int> tmp(2 * n);
+    cudaMemcpy(tmp.data(), buf, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost);
+    std::vector<std::pair<int, int>> v(n);
+    for (size_t p = 0; p < n; p++) v[p] = {tmp[2 * p], tmp[2 * p + 1]};
+    std::sort(v.begin(), v.end());
+    for (size_t p = 0; p < n; p++) {
+      pairs[2 * p] = v[p].first;
+      pairs[2 * p + 1] = v[p].second;
+    }
+  }
+  cudaFree(cnt);
+  cudaFree(buf);
+  return rc;
+}
+
+int rdsim_get_cell_ids(rdsim_handle* h, int32_t sys, int32_t* cell_ids) {
+  if (!h || sys < 0 || sys >= h->nsys || !cell_ids) return fail(RDSIM_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  const HostSys& q = h->hs[sys];
+  int* buf = nullptr;
+  CK(cudaMalloc(&buf, sizeof(int) * (size_t)q.n * h->D));
+  Args a = make_args(h);
+  unsigned g = nblk(q.n);
+  const double* cl = h->cl_d + 3 * sys;
+  if (h->D == 2) k_ref_cells<2><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, cl, q.p0, q.n, q.pid0, buf);
+  else if (h->D == 3) k_ref_cells<3><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, cl, q.p0, q.n, q.pid0, buf);
+  else k_ref_cells<1><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, cl, q.p0, q.n, q.pid0, buf);
+  cudaError_t e1 = cudaGetLastError();
+  cudaMemcpyAsync(cell_ids, buf, sizeof(int) * (size_t)q.n * h->D, cudaMemcpyDeviceToHost, h->stream);
+  cudaStreamSynchronize(h->stream);
+  cudaFree(buf);
+  if (e1 != cudaSuccess) return fail(RDSIM_ERR_CUDA, cudaGetErrorString(e1));
+  return 0;
+}
+
+int rdsim_get_step(rdsim_handle* h, int64_t* step) {
+  if (!h || !step) return fail(RDSIM_ERR_ARG, "null argument");
+  *step = h->step;
+  return 0;
+}
+
+int rdsim_set_step(rdsim_handle* h, int64_t step) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  h->step = step;
+  return 0;
+}
+
+int rdsim_set_trajectory(rdsim_handle* h, int32_t stride, int32_t n_frames) {
+  if (!h || stride <= 0 || n_frames < 0) return fail(RDSIM_ERR_ARG, "bad trajectory arguments");
+  CK(cudaSetDevice(h->device));
+  if (h->traj_x) cudaFree(h->traj_x);
+  if (h->traj_t) cudaFree(h->traj_t);
+  h->traj_x = nullptr;
+  h->traj_t = nullptr;
+  h->traj_stride = stride;
+  h->traj_frames = n_frames;
+  if (n_frames == 0) return 0;
+  int64_t dummy = 0;
+  int rc;
+  if ((rc = dalloc(&h->traj_x, (size_t)n_frames * h->N * h->D, &dummy))) return rc;
+  if ((rc = dalloc(&h->traj_t, (size_t)n_frames * h->N, &dummy))) return rc;
+  CK(cudaMemsetAsync(h->traj_x, 0, sizeof(double) * (size_t)n_frames * h->N * h->D, h->stream));
+  CK(cudaMemsetAsync(h->traj_t, 0, sizeof(int) * (size_t)n_frames * h->N, h->stream));
+  return 0;
+}
+
+int rdsim_get_trajectory(rdsim_handle* h, double* x, int32_t* types) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  if (h->traj_frames == 0) return 0;
+  CK(cudaSetDevice(h->device));
+  size_t nx = (size_t)h->traj_frames * h->N * h->D, nt = (size_t)h->traj_frames * h->N;
+  if (x) CK(cudaMemcpyAsync(x, h->traj_x, sizeof(double) * nx, cudaMemcpyDeviceToHost, h->stream));
+  if (types) CK(cudaMemcpyAsync(types, h->traj_t, sizeof(int) * nt, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int rdsim_get_error(rdsim_handle* h, int32_t* code, int64_t* particle, int32_t* dim,
+                    double* value, int64_t* step) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  ErrDev e;
+  CK(cudaMemcpyAsync(&e, h->err, sizeof e, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemsetAsync(h->err, 0, sizeof e, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (code) *code = e.code;
+  if (particle) *particle = e.particle;
+  if (dim) *dim = e.dim;
+  if (value) *value = e.value;
+  if (step) *step = e.step;
+  return 0;
+}
+
+int rdsim_get_stream(rdsim_handle* h, void** stream) {
+  if (!h || !stream) return fail(RDSIM_ERR_ARG, "null argument");
+  *stream = (void*)h->stream;
+  return 0;
+}
+
+int rdsim_set_profiling(rdsim_handle* h, int32_t enable) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  h->prof = enable != 0;
+  return 0;
+}
+
+int rdsim_get_profile(rdsim_handle* h, rdsim_profile* p) {
+  if (!h || !p) return fail(RDSIM_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  resolve_profile(h);
+  for (int c = 0; c < RDSIM_PROFILE_CLASSES; c++) {
+    p->launches[c] = h->nlaunch[c];
+    p->ms[c] = h->prof_ms[c];
+    p->timed[c] = h->prof_n[c];
+    h->nlaunch[c] = 0;
+    h->prof_ms[c] = 0;
+    h->prof_n[c] = 0;
+  }
+  return 0;
+}
+
+int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
+  if (!h || !info) return fail(RDSIM_ERR_ARG, "null argument");
+  std::memset(info, 0, sizeof *info);
+  info->n_particles = h->N;
+  info->n_cells = h->ncells;
+  info->n_tiles = (int64_t)h->tiles_h.size();
+  info->threads_per_particle = h->tpp;
+  info->max_tile_particles = h->cap;
+  info->skin = h->skin;
+  info->cell_size_min = h->cell_min;
+  info->interaction_range = h->range;
+  info->device_bytes = h->device_bytes;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,934 @@
+// kernels.cuh -- sm_103a kernels of the simulation step.
+//
+//   k_bin / k_scan_* / k_scatter / k_order : cell-list rebuild, a warp-
+//       aggregated counting sort of all systems' particles into cells
+//       (replaces create_neighbor_list, pyrdsim.pyx:1448-1587)
+//   k_react<D,TPP>  : neighbourhood-dependent reaction propensities and the
+//       draws that flip particle types (reaction_step, pyrdsim.pyx:2070-2223)
+//   k_force<D,TPP>  : pair + wall + bonded drift (update_drifts,
+//       pyrdsim.pyx:1941-2067), optionally fused with the next step's
+//       Euler-Maruyama update and boundary conditions (pyrdsim.pyx:2225-2292)
+//   k_em<D>         : stand-alone Euler-Maruyama update
+//   hooks           : reference cell ids, neighbour pairs, snapshots
+//
+// Tile kernels: one CTA per tile of cells of one system.  The CTA stages the
+// tile plus a one-cell halo (cell-sorted, so every halo row of cells is one
+// contiguous range) into shared memory, then TPP threads share each own
+// particle's candidate loop and combine with warp shuffles.  If a tile's
+// halo exceeds the shared-memory capacity the same loop reads global memory.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace rd {
+
+__device__ inline void record_error(ErrDev* e, int code, long long particle, int dim,
+                                    double value, long long step) {
+  if (atomicCAS(&e->code, 0, code) == 0) {
+    e->particle = particle;
+    e->dim = dim;
+    e->value = value;
+    e->step = step;
+  }
+}
+
+__device__ inline double fixed_to_double(const SysDev& s, int k, uint32_t h, uint32_t l) {
+  unsigned long long X = ((unsigned long long)h << 32) | l;
+  if ((s.periodic >> k) & 1) return __dmul_rn(__ull2double_rn(X), s.unit_d[k]);
+  return __dmul_rn(__ll2double_rn((long long)X), s.unit_d[k]);
+}
+
+// Distance of two particles exactly as pyrdsim.pyx:1619-1633 computes it
+// (float64, C round() minimum image, pow(v, 2) summed in dimension order).
+template <int D>
+__device__ double exact_dist(const SysDev& s, const Args& a, int gi, int gj) {
+  double d2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    double xi = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
+    double xj = fixed_to_double(s, k, a.xh[k][gj], a.xl[k][gj]);
+    double v = __dsub_rn(xj, xi);
+    if ((s.periodic >> k) & 1) v = __dsub_rn(v, __dmul_rn(s.L[k], round(__ddiv_rn(v, s.L[k]))));
+    d2 = __dadd_rn(d2, __dmul_rn(v, v));
+  }
+  return __dsqrt_rn(d2);
+}
+
+// f / r of one pair law at squared distance r2 (float32).
+__device__ inline float eval_pair(const PairLaw& L, float r2) {
+  switch (L.law) {
+    case RDSIM_LAW_LJ: {  // f = -2 n u0 / r * s (s - 1), s = (r0/r)^n
+      float q = L.c1 / r2;  // (r0/r)^2
+      float s;
+      if ((L.n & 1) == 0) {
+        s = 1.0f;
+        for (int e = 0; e < (L.n >> 1); e++) s *= q;
+      } else {
+        float b = sqrtf(q);
+        s = 1.0f;
+        for (int e = 0; e < L.n; e++) s *= b;
+      }
+      return L.c0 * s * (s - 1.0f) / r2;
+    }
+    case RDSIM_LAW_TANH: {  // f = u0 (1 - tanh^2 z) / (2a), z = (r - r0)/a
+      float r = sqrtf(r2);
+      float z = (r - L.c1) * L.c2;
+      float e = expf(-2.0f * fabsf(z));
+      float sech2 = 4.0f * e / ((1.0f + e) * (1.0f + e));
+      return L.c0 * sech2 / r;
+    }
+    case RDSIM_LAW_YUKAWA: {  // f = -u0 (1 + r0/r) exp(-r/r0) / (r r0)
+      float r = sqrtf(r2);
+      return L.c0 * (1.0f + L.c1 / r) * expf(-r * L.c2) / r2;
+    }
+    case RDSIM_LAW_HARMONIC:  // f = u0 r
+      return L.c0;
+    case RDSIM_LAW_PIECEWISE_LINEAR: {  // f = u0/dr for r >= r0 - dr
+      return L.c0 / sqrtf(r2);
+    }
+  }
+  return 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive scan of MAXHC ints held two per thread (BLOCK = 128).
+__device__ inline void scan_pairs(int* v, int* warp_tmp, int* total) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  int a0 = v[2 * tid], a1 = v[2 * tid + 1];
+  int s = a0 + a1, inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) warp_tmp[w] = inc;
+  __syncthreads();
+  int off = 0;
+  for (int q = 0; q < w; q++) off += warp_tmp[q];
+  int ex = off + inc - s;
+  if (tid == BLOCK - 1) *total = ex + s;
+  __syncthreads();
+  v[2 * tid] = ex;
+  v[2 * tid + 1] = ex + a0;
+  __syncthreads();
+}
+
+// last index q in [0, n) with arr[q] <= key (arr non-decreasing, arr[0] <= key)
+__device__ inline int last_le(const int* arr, int n, int key) {
+  int lo = 0, hi = n;  // answer in [lo, hi)
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (arr[mid] <= key) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int D>
+struct TileShared {
+  SysDev sys;
+  PairLaw laws[MAXI];
+  WallLaw walls[MAXW];
+  RxDev rx[MAXR];
+  int beg[MAXHC];
+  int cnt[MAXHC];
+  int gbeg[MAXHC];
+  int own[MAXHC];
+  int warp_tmp[BLOCK / 32];
+  int hdim[3];
+  int nhc, total, nown, use_smem;
+};
+
+template <int D>
+struct Staged {
+  const uint32_t* xh[D];
+  const uint32_t* meta;
+  const int* mol;
+  const int* gi;  // null: index is already global
+};
+
+// Copy the system tables and stage the tile's halo.  Returns the source
+// arrays (shared memory, or global memory when the halo does not fit).
+template <int D>
+__device__ Staged<D> tile_setup(TileShared<D>& sh, const Args& a, const Tile& t,
+                                uint32_t* dyn) {
+  const int tid = threadIdx.x;
+  {
+    const int* src = reinterpret_cast<const int*>(&a.sys[t.sys]);
+    int* dst = reinterpret_cast<int*>(&sh.sys);
+    for (int q = tid; q < (int)(sizeof(SysDev) / 4); q += BLOCK) dst[q] = src[q];
+  }
+  __syncthreads();
+  const SysDev& s = sh.sys;
+  {
+    const int* src = reinterpret_cast<const int*>(a.laws + s.law0);
+    int* dst = reinterpret_cast<int*>(sh.laws);
+    int nw = s.nlaws * (int)(sizeof(PairLaw) / 4);
+    for (int q = tid; q < nw; q += BLOCK) dst[q] = src[q];
+    src = reinterpret_cast<const int*>(a.walls + s.wall0);
+    dst = reinterpret_cast<int*>(sh.walls);
+    nw = s.nwalls * (int)(sizeof(WallLaw) / 4);
+    for (int q = tid; q < nw; q += BLOCK) dst[q] = src[q];
+    src = reinterpret_cast<const int*>(a.rx + s.rx0);
+    dst = reinterpret_cast<int*>(sh.rx);
+    nw = s.nrx * (int)(sizeof(RxDev) / 4);
+    for (int q = tid; q < nw; q += BLOCK) dst[q] = src[q];
+  }
+  if (tid == 0) {
+    int n = 1;
+    for (int k = 0; k < D; k++) {
+      sh.hdim[k] = t.w[k] + 2 * s.halo[k];
+      n *= sh.hdim[k];
+    }
+    sh.nhc = n;
+  }
+  __syncthreads();
+  const int nhc = sh.nhc;
+  for (int q = tid; q < MAXHC; q += BLOCK) {
+    int c = 0, g = 0, interior = 0;
+    if (q < nhc) {
+      bool inb = true;
+      interior = 1;
+      int rem = q, mult = 1;
+      for (int k = 0; k < D; k++) {
+        int hc = rem % sh.hdim[k];
+        rem /= sh.hdim[k];
+        if (hc < s.halo[k] || hc >= s.halo[k] + t.w[k]) interior = 0;
+        int ck = t.c[k] - s.halo[k] + hc;
+        if ((s.periodic >> k) & 1) {
+          if (ck < 0) ck += s.nc[k];
+          if (ck >= s.nc[k]) ck -= s.nc[k];
+        } else if (ck < 0 || ck >= s.nc[k]) {
+          inb = false;
+        }
+        g += ck * mult;
+        mult *= s.nc[k];
+      }
+      if (inb) {
+        int b = a.cell_start[s.c0 + g];
+        c = a.cell_start[s.c0 + g + 1] - b;
+        sh.gbeg[q] = b;
+      } else {
+        sh.gbeg[q] = 0;
+      }
+    }
+    sh.cnt[q] = c;
+    sh.beg[q] = c;
+    sh.own[q] = interior ? c : 0;
+  }
+  __syncthreads();
+  int total, nown;
+  scan_pairs(sh.beg, sh.warp_tmp, &sh.total);
+  total = sh.total;
+  scan_pairs(sh.own, sh.warp_tmp, &sh.nown);
+  nown = sh.nown;
+  (void)nown;
+  const bool use_smem = total <= a.cap;
+  Staged<D> st;
+  if (use_smem) {
+    uint32_t* sx = dyn;
+    uint32_t* smeta = dyn + D * a.cap;
+    int* smol = reinterpret_cast<int*>(dyn + (D + 1) * a.cap);
+    int* sgi = reinterpret_cast<int*>(dyn + (D + 2) * a.cap);
+    for (int e = tid; e < total; e += BLOCK) {
+      int q = last_le(sh.beg, nhc, e);
+      int src = sh.gbeg[q] + (e - sh.beg[q]);
+#pragma unroll
+      for (int k = 0; k < D; k++) sx[k * a.cap + e] = a.xh[k][src];
+      smeta[e] = a.meta[src];
+      smol[e] = a.mol[src];
+      sgi[e] = src;
+    }
+#pragma unroll
+    for (int k = 0; k < D; k++) st.xh[k] = sx + k * a.cap;
+    st.meta = smeta;
+    st.mol = smol;
+    st.gi = sgi;
+  } else {
+    for (int q = tid; q < nhc; q += BLOCK) sh.beg[q] = sh.gbeg[q];
+#pragma unroll
+    for (int k = 0; k < D; k++) st.xh[k] = a.xh[k];
+    st.meta = a.meta;
+    st.mol = a.mol;
+    st.gi = nullptr;
+  }
+  if (tid == 0) sh.use_smem = use_smem ? 1 : 0;
+  __syncthreads();
+  return st;
+}
+
+// Visit every candidate neighbour of the own particle in halo cell `q`:
+// the 3^D (or fewer) cells around it.  fn(j) is called with the source index.
+template <int D, int TPP, class Fn>
+__device__ inline void for_candidates(const TileShared<D>& sh, int q, int lane_g, Fn&& fn) {
+  const SysDev& s = sh.sys;
+  int hc[3] = {0, 0, 0};
+  {
+    int rem = q;
+    for (int k = 0; k < D; k++) {
+      hc[k] = rem % sh.hdim[k];
+      rem /= sh.hdim[k];
+    }
+  }
+  const int h0 = s.halo[0];
+  const int h1 = D > 1 ? s.halo[1] : 0;
+  const int h2 = D > 2 ? s.halo[2] : 0;
+  for (int dz = -h2; dz <= h2; dz++) {
+    for (int dy = -h1; dy <= h1; dy++) {
+      int rowbase = 0;
+      if (D == 2) rowbase = (hc[1] + dy) * sh.hdim[0];
+      if (D == 3) rowbase = ((hc[2] + dz) * sh.hdim[1] + (hc[1] + dy)) * sh.hdim[0];
+      int qa = rowbase + hc[0] - h0, qb = rowbase + hc[0] + h0;
+      if (sh.use_smem) {
+        int b = sh.beg[qa], e = sh.beg[qb] + sh.cnt[qb];
+        for (int j = b + lane_g; j < e; j += TPP) fn(j);
+      } else {
+        for (int qq = qa; qq <= qb; qq++) {
+          int b = sh.beg[qq], e = b + sh.cnt[qq];
+          for (int j = b + lane_g; j < e; j += TPP) fn(j);
+        }
+      }
+    }
+  }
+}
+
+__device__ inline long long delta_fixed(float d, float inv_unit_hi, bool* bad) {
+  float v = d * inv_unit_hi;
+  if (!(fabsf(v) < 1073741824.0f)) {  // non-finite or > a quarter box
+    *bad = true;
+    return 0;
+  }
+  float fl = floorf(v);
+  int hi = (int)fl;
+  float frac = v - fl;
+  unsigned int lo = __float2uint_rn(frac * 4294967296.0f);
+  return (long long)hi * 4294967296LL + (long long)lo;
+}
+
+__device__ inline double uniform53(uint32_t hi, uint32_t lo) {
+  unsigned long long m = (((unsigned long long)hi << 32) | lo) >> 11;
+  return __dadd_rn(__dmul_rn(__ull2double_rn(m), 1.1102230246251565e-16), 5.551115123125783e-17);
+}
+
+template <int D>
+__device__ inline void gaussians(unsigned long long seed, long long step, int pid, float* xi) {
+  U4 w = noise_words(seed, step, pid, 0u);
+  float ua = (float)w.x * 2.3283064365386963e-10f + 1.1641532182693481e-10f;
+  float r = sqrtf(-2.0f * logf(ua));
+  float sn, cs;
+  sincospif(2.0f * ((float)w.y * 2.3283064365386963e-10f), &sn, &cs);
+  xi[0] = r * cs;
+  if (D > 1) xi[1] = r * sn;
+  if (D > 2) {
+    float ub = (float)w.z * 2.3283064365386963e-10f + 1.1641532182693481e-10f;
+    float r2 = sqrtf(-2.0f * logf(ub));
+    float s2, c2;
+    sincospif(2.0f * ((float)w.w * 2.3283064365386963e-10f), &s2, &c2);
+    xi[2] = r2 * c2;
+  }
+}
+
+// Euler-Maruyama update + boundary conditions of one particle in fixed point
+// (pyrdsim.pyx:2240-2292): x += dt D a + sqrt(2 dt D) xi, then reflect or wrap.
+template <int D>
+__device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid, int type,
+                                 const float* acc, long long em_step, int flags) {
+  float xi[3] = {0.f, 0.f, 0.f};
+  if (!(flags & F_NO_NOISE)) {
+    if (flags & F_INJECT) {
+#pragma unroll
+      for (int k = 0; k < D; k++) xi[k] = (float)a.xi[(size_t)pid * D + k];
+    } else {
+      gaussians<D>(s.seed, em_step, pid, xi);
+    }
+  }
+  const float fp = s.fp[type], np = s.npf[type];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    bool bad = false;
+    float dl = fp * acc[k] + np * xi[k];
+    long long d = delta_fixed(dl, s.inv_unit_hi[k], &bad);
+    unsigned long long X = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
+    if (bad) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)dl, em_step);
+    if ((s.periodic >> k) & 1) {
+      X += (unsigned long long)d;
+    } else {
+      long long Xs = (long long)X + d;
+      long long Si = s.Si[k];
+      if (Xs > Si) Xs = 2 * Si - Xs;
+      if (Xs < 0) Xs = -Xs;
+      if (Xs < 0 || Xs > Si) {
+        record_error(a.err, RDSIM_ERR_OUT_OF_BOUNDS, pid, k,
+                     __dmul_rn(__ll2double_rn(Xs), s.unit_d[k]), em_step);
+        Xs = Xs < 0 ? 0 : Si;
+      }
+      X = (unsigned long long)Xs;
+    }
+    a.xh_out[k][gi] = (uint32_t)(X >> 32);
+    a.xl_out[k][gi] = (uint32_t)X;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Drift kernel.
+template <int D, int TPP>
+__global__ void __launch_bounds__(BLOCK) k_force(Args a) {
+  extern __shared__ uint32_t dyn[];
+  __shared__ TileShared<D> sh;
+  const Tile t = a.tiles[blockIdx.x];
+  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
+  const SysDev& s = sh.sys;
+  const int tid = threadIdx.x;
+  const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
+  const int nhc = sh.nhc, nown = sh.nown;
+  for (int p0 = 0; p0 < nown; p0 += groups) {
+    const int p = p0 + g;
+    const bool active = p < nown;
+    float acc[3] = {0.f, 0.f, 0.f};
+    int q = 0, idx = 0, gi = 0;
+    uint32_t mi = 0;
+    if (active) {
+      q = last_le(sh.own, nhc, p);
+      idx = sh.beg[q] + (p - sh.own[q]);
+      gi = st.gi ? st.gi[idx] : idx;
+      uint32_t xi_h[3];
+#pragma unroll
+      for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
+      mi = st.meta[idx];
+      const int moli = st.mol[idx];
+      const int ti = mi & 0xff, trbi = (mi >> 8) & 0xff;
+      const unsigned int pmask = s.partner[trbi];
+      if (s.R2 > 0.f) for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
+        float dx[3], r2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          dx[k] = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
+          r2 += dx[k] * dx[k];
+        }
+        if (!(r2 < s.R2)) return;
+        if (st.mol[j] == moli) return;  // same molecule (and self)
+        const uint32_t mj = st.meta[j];
+        const int tj = mj & 0xff, trbj = (mj >> 8) & 0xff;
+        if (!((pmask >> trbj) & 1)) return;
+        const unsigned int pp = s.ppair[ti * MAXT + tj];
+        const int nl = pp & 31, l0 = pp >> 5;
+        if (!nl) return;
+        float fr = 0.f;
+        double dexact = -1.0;
+        for (int l = l0; l < l0 + nl; l++) {
+          const PairLaw& L = sh.laws[l];
+          if (r2 > L.rc2_hi) continue;
+          if (r2 >= L.rc2_lo) {
+            if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+            if (dexact > L.rc) continue;
+          }
+          if (L.law == RDSIM_LAW_PIECEWISE_LINEAR) {
+            if (r2 < L.in2_lo) continue;
+            if (r2 <= L.in2_hi) {
+              if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+              if (dexact < L.rin) continue;
+            }
+          }
+          fr += eval_pair(L, r2);
+        }
+#pragma unroll
+        for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
+      });
+    }
+#pragma unroll
+    for (int o = TPP >> 1; o > 0; o >>= 1) {
+#pragma unroll
+      for (int k = 0; k < D; k++) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    }
+    if (!active || lane_g != 0) continue;
+    const int ti = mi & 0xff;
+    const int pid = a.pid[gi];
+    // walls (pyrdsim.pyx:1979-1986)
+    for (int w = 0; w < s.nwalls; w++) {
+      const WallLaw& W = sh.walls[w];
+      if (W.type != ti) continue;
+      const uint32_t h = a.xh[W.dim][gi];
+      float f;
+      if (W.law == RDSIM_LAW_WALL) {
+        float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
+        float e = expf(-2.0f * fabsf(z));
+        f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
+      } else {
+        float y = (float)h * s.unit_hi[W.dim];
+        if (y > W.rc_hi) continue;
+        if (y >= W.rc_lo) {
+          double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
+          if (yd > W.rc) continue;
+        }
+        float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
+        f = W.c0 / y * (-1.2f * s9 + 3.0f * s3);
+      }
+#pragma unroll
+      for (int k = 0; k < D; k++)
+        if (k == W.dim) acc[k] += -f;
+    }
+    // bonded terms (pyrdsim.pyx:2037-2066), gathered per participant
+    const int tm = mi >> 24;
+    if (tm != 0xff) {
+      const TmplDev& T = a.tmpl[tm];
+      const int loc = (mi >> 16) & 0xff;
+      const int base = pid - loc;
+      float xo[3];
+      for (int e = a.atomterm[T.atom0 + loc]; e < a.atomterm[T.atom0 + loc + 1]; e++) {
+        const int code = a.atomterm[e];
+        const TermDev& tr = a.terms[code >> 2];
+        const int role = code & 3;
+        if (tr.kind == RDSIM_TERM_BOND) {
+          const int other = a.slot_of[base + (role == 0 ? tr.j : tr.i)];
+          float d2 = 0.f;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            xo[k] = (float)(int)(a.xh[k][other] - a.xh[k][gi]) * s.unit_hi[k];
+            d2 += xo[k] * xo[k];
+          }
+          const float d = sqrtf(d2);
+          const float f = tr.k0 * (d - tr.p0) / d;
+#pragma unroll
+          for (int k = 0; k < D; k++) acc[k] += f * xo[k];
+        } else {
+          const int s1 = a.slot_of[base + tr.i], s2 = a.slot_of[base + tr.j],
+                    s3 = a.slot_of[base + tr.k];
+          float v1[3], v2[3], n1 = 0.f, n2 = 0.f;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            v1[k] = (float)(int)(a.xh[k][s1] - a.xh[k][s2]) * s.unit_hi[k];
+            v2[k] = (float)(int)(a.xh[k][s3] - a.xh[k][s2]) * s.unit_hi[k];
+            n1 += v1[k] * v1[k];
+            n2 += v2[k] * v2[k];
+          }
+          const float d21 = sqrtf(n1), d23 = sqrtf(n2);
+          float c = 0.f, sn;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            v1[k] /= d21;
+            v2[k] /= d23;
+            c += v1[k] * v2[k];
+          }
+          if (D == 2) {
+            sn = fabsf(v1[0] * v2[1] - v1[1] * v2[0]);
+          } else {
+            float cx = v1[1] * v2[2] - v1[2] * v2[1];
+            float cy = v1[2] * v2[0] - v1[0] * v2[2];
+            float cz = v1[0] * v2[1] - v1[1] * v2[0];
+            sn = sqrtf(cx * cx + cy * cy + cz * cz);
+          }
+          const float theta = atan2f(sn, c);
+          float prefac;
+          if (s.angle_is_pi > 0 && !(theta < tr.thr)) {
+            const float dt_ = theta - tr.p0, d2_ = dt_ * dt_;
+            prefac = -tr.k0 / (1.0f - d2_ / 6.0f + d2_ * d2_ / 120.0f);
+          } else {
+            prefac = tr.k0 * (theta - tr.p0) / sn;
+          }
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            const float f1 = prefac / d21 * (v2[k] - c * v1[k]);
+            const float f3 = prefac / d23 * (v1[k] - c * v2[k]);
+            acc[k] += role == 0 ? f1 : (role == 2 ? f3 : -(f1 + f3));
+          }
+        }
+      }
+    }
+    if (a.flags & F_STORE_DRIFT) {
+#pragma unroll
+      for (int k = 0; k < D; k++) a.drift[k][gi] = acc[k];
+    }
+#pragma unroll
+    for (int k = 0; k < D; k++)
+      if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], a.step);
+    if (a.flags & F_CHECK_SKIN) {
+      // displacement since the last rebuild: keeps every pair within range in
+      // adjacent cells and within rs of each other at that rebuild
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        float rel = fabsf((float)(int)(a.xh[k][gi] - a.xr[k][gi])) * s.unit_hi[k];
+        if (rel > s.delta)
+          record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, a.step);
+      }
+    }
+    if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, a.em_step, a.flags);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reaction kernel: propensities from the current types, draws, new types.
+template <int D, int TPP>
+__global__ void __launch_bounds__(BLOCK) k_react(Args a) {
+  const TmplDev* tmpl = a.tmpl;
+  extern __shared__ uint32_t dyn[];
+  __shared__ TileShared<D> sh;
+  const Tile t = a.tiles[blockIdx.x];
+  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
+  const SysDev& s = sh.sys;
+  const int tid = threadIdx.x;
+  const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
+  const int nhc = sh.nhc, nown = sh.nown;
+  for (int p0 = 0; p0 < nown; p0 += groups) {
+    const int p = p0 + g;
+    const bool active = p < nown;
+    int cnt[MAXR];
+#pragma unroll
+    for (int r = 0; r < MAXR; r++) cnt[r] = 0;
+    int idx = 0, gi = 0;
+    uint32_t mi = 0;
+    if (active) {
+      const int q = last_le(sh.own, nhc, p);
+      idx = sh.beg[q] + (p - sh.own[q]);
+      gi = st.gi ? st.gi[idx] : idx;
+      mi = st.meta[idx];
+      const int ti = mi & 0xff;
+      if ((s.rx_nb_mask >> ti) & 1) {
+        uint32_t xi_h[3];
+#pragma unroll
+        for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
+        const int moli = st.mol[idx];
+        const int trbi = (mi >> 8) & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
+        const unsigned int pmask = s.partner[trbi];
+        const uint32_t bmask = tmi != 0xff ? tmpl[tmi].bondmask[loci] : 0u;
+        for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
+          if (j == idx) return;
+          float r2 = 0.f;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            float dx = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
+            r2 += dx * dx;
+          }
+          if (!(r2 < s.Rrx2)) return;
+          const uint32_t mj = st.meta[j];
+          bool listed;
+          if (st.mol[j] == moli) listed = (bmask >> ((mj >> 16) & 31)) & 1;
+          else listed = (pmask >> ((mj >> 8) & 0xff)) & 1;
+          if (!listed) return;
+          const int tj = mj & 0xff;
+          double dexact = -1.0;
+#pragma unroll
+          for (int r = 0; r < MAXR; r++) {
+            if (r >= s.nrx) break;
+            const RxDev& R = sh.rx[r];
+            if (R.reactant != ti) continue;
+            bool match = (R.kind == RDSIM_RX_CATALYZED && tj == R.catalyst) ||
+                         (R.kind == RDSIM_RX_INHIBITED && (tj == R.inh || tj == R.inh2));
+            if (!match) continue;
+            bool inside;
+            if (r2 < R.r02_lo) inside = true;
+            else if (r2 > R.r02_hi) inside = false;
+            else {
+              if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+              inside = dexact < R.r0;
+            }
+            cnt[r] += inside ? 1 : 0;
+          }
+        });
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < MAXR; r++)
+#pragma unroll
+      for (int o = TPP >> 1; o > 0; o >>= 1) cnt[r] += __shfl_xor_sync(0xffffffffu, cnt[r], o);
+    if (!active || lane_g != 0) continue;
+    const int ti = mi & 0xff;
+    int newt = ti;
+    double total = 0.0;
+    double rate[MAXR];
+#pragma unroll
+    for (int r = 0; r < MAXR; r++) {  // pyrdsim.pyx:2091-2206, file order
+      rate[r] = 0.0;
+      if (r >= s.nrx) continue;
+      const RxDev& R = sh.rx[r];
+      double v = 0.0;
+      if (R.reactant == ti) {
+        if (R.kind == RDSIM_RX_LINEAR) {
+          v = R.rate;
+          total = __dadd_rn(total, R.rate);
+        } else if (R.kind == RDSIM_RX_CATALYZED) {
+          for (int c = 0; c < cnt[r]; c++) {
+            v = __dadd_rn(v, R.rate);
+            total = __dadd_rn(total, R.rate);
+          }
+        } else {
+          v = R.rate;
+          for (int c = 0; c < cnt[r]; c++) v = __dsub_rn(v, R.dec);
+          if (v < 0) v = 0.0;
+          total = __dadd_rn(total, v);
+        }
+      }
+      rate[r] = v;
+    }
+    if (a.flags & F_RATES_ONLY) {
+      a.rates_out[a.pid[gi]] = total;
+      continue;
+    }
+    if ((s.rx_any_mask >> ti) & 1) {  // pyrdsim.pyx:2211-2222
+      const int pid = a.pid[gi];
+      double u1, u2;
+      U4 w;
+      if (a.flags & F_INJECT) {
+        u1 = a.u1[pid];
+      } else {
+        w = noise_words(s.seed, a.step, pid, 1u);
+        u1 = uniform53(w.x, w.y);
+      }
+      if (__dmul_rn(s.dt, total) > u1) {
+        u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
+        double acc = 0.0;
+        bool done = false;
+#pragma unroll
+        for (int r = 0; r < MAXR; r++) {
+          if (r >= s.nrx || done) continue;
+          acc = __dadd_rn(acc, __ddiv_rn(rate[r], total));
+          if (acc >= u2) {
+            newt = sh.rx[r].product;
+            done = true;
+          }
+        }
+      }
+    }
+    a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stand-alone EM update of every particle (first step of a call).
+template <int D>
+__global__ void k_em(Args a, const int* sid) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= a.n_total) return;
+  const SysDev& s = a.sys[sid[gi]];
+  float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < D; k++) acc[k] = a.drift[k][gi];
+  em_update<D>(s, a, gi, a.pid[gi], a.meta[gi] & 0xff, acc, a.em_step, a.flags);
+}
+
+// ---------------------------------------------------------------------------
+// Cell-list rebuild.
+template <int D>
+__global__ void k_bin(const SysDev* sysv, const int* sid, const uint32_t* x0, const uint32_t* x1,
+                      const uint32_t* x2, int n, int* cell_of, int* rank_of, int* count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool valid = i < n;
+  int gcell = -1 - lane;
+  if (valid) {
+    const SysDev& s = sysv[sid[i]];
+    const uint32_t* xs[3] = {x0, x1, x2};
+    int g = 0, mult = 1;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      unsigned long long h = xs[k][i];
+      int c = (int)((h * (unsigned long long)s.nc[k]) / s.hrange[k]);
+      if (c >= s.nc[k]) c = s.nc[k] - 1;
+      if (c < 0) c = 0;
+      g += c * mult;
+      mult *= s.nc[k];
+    }
+    gcell = s.c0 + g;
+  }
+  const unsigned int peers = __match_any_sync(0xffffffffu, gcell);
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (valid && lane == leader) base = atomicAdd(&count[gcell], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (valid) {
+    cell_of[i] = gcell;
+    rank_of[i] = base + __popc(peers & ((1u << lane) - 1u));
+  }
+}
+
+// Exclusive scan of count[0..n) into start[0..n]; two passes, no waits.
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = 256 * SCAN_ITEMS;
+
+__global__ void k_scan_partial(const int* count, int n, int* bsum) {
+  __shared__ int ws[8];
+  const int base = blockIdx.x * SCAN_TILE;
+  int s = 0;
+  for (int e = threadIdx.x; e < SCAN_TILE; e += 256) {
+    int q = base + e;
+    if (q < n) s += count[q];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < 8; w++) t += ws[w];
+    bsum[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_scan_final(const int* count, int n, const int* bsum, int* start) {
+  __shared__ int ws[8];
+  __shared__ int prefix;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  int p = 0;
+  for (int b = tid; b < (int)blockIdx.x; b += 256) p += bsum[b];
+  for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+  if (lane == 0) ws[w] = p;
+  __syncthreads();
+  if (tid == 0) {
+    int t = 0;
+    for (int q = 0; q < 8; q++) t += ws[q];
+    prefix = t;
+  }
+  __syncthreads();
+  const int base = blockIdx.x * SCAN_TILE + tid * SCAN_ITEMS;
+  int v[SCAN_ITEMS], sum = 0;
+#pragma unroll
+  for (int e = 0; e < SCAN_ITEMS; e++) {
+    v[e] = (base + e < n) ? count[base + e] : 0;
+    sum += v[e];
+  }
+  int inc = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  __syncthreads();
+  if (lane == 31) ws[w] = inc;
+  __syncthreads();
+  int off = prefix;
+  for (int q = 0; q < w; q++) off += ws[q];
+  int run = off + inc - sum;
+#pragma unroll
+  for (int e = 0; e < SCAN_ITEMS; e++) {
+    if (base + e < n) start[base + e] = run;
+    run += v[e];
+  }
+  // items past n count as zero, so the last thread of the grid holds the total
+  if (blockIdx.x == gridDim.x - 1 && tid == 255) start[n] = run;
+}
+
+__global__ void k_scatter(const int* cell_of, const int* rank_of, const int* start, int n,
+                          int* tmp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  tmp[start[cell_of[i]] + rank_of[i]] = i;
+}
+
+// Deterministic order inside each cell (by caller index), then gather every
+// per-particle array into its final slot.  Records types at this rebuild.
+struct OrderOut {
+  int* mol;
+  int* pid;
+  uint32_t* xr[3];
+  int* slot_of;
+};
+
+template <int D>
+__global__ void k_order(Args a, OrderOut o, const int* tmp, const int* cell_of,
+                        const int* start, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int old = tmp[k];
+  const int g = cell_of[old];
+  const int b = start[g], e = start[g + 1];
+  const int myid = a.pid[old];
+  int fin = k;
+  if (e - b <= 1024) {  // larger cells keep the atomic order
+    int r = 0;
+    for (int q = b; q < e; q++) r += a.pid[tmp[q]] < myid ? 1 : 0;
+    fin = b + r;
+  }
+#pragma unroll
+  for (int d = 0; d < D; d++) {
+    const uint32_t h = a.xh[d][old];
+    a.xh_out[d][fin] = h;
+    a.xl_out[d][fin] = a.xl[d][old];
+    o.xr[d][fin] = h;
+  }
+  const uint32_t m = a.meta[old];
+  a.meta_out[fin] = (m & 0xffff00ffu) | ((m & 0xffu) << 8);
+  o.mol[fin] = a.mol[old];
+  o.pid[fin] = myid;
+  o.slot_of[myid] = fin;
+}
+
+// ---------------------------------------------------------------------------
+// Hooks (tests and reports).
+template <int D>
+__global__ void k_to_double(const SysDev* sysv, const int* sid, Args a, double* x, int* types) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= a.n_total) return;
+  const SysDev& s = sysv[sid[gi]];
+  const int pid = a.pid[gi];
+#pragma unroll
+  for (int k = 0; k < D; k++) x[(size_t)pid * D + k] = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
+  if (types) types[pid] = a.meta[gi] & 0xff;
+}
+
+// trajectory frame: positions (float64) and types in caller order
+template <int D>
+__global__ void k_snapshot(const SysDev* sysv, const int* sid, Args a, double* fx, int* ft) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= a.n_total) return;
+  const SysDev& s = sysv[sid[gi]];
+  const int pid = a.pid[gi];
+#pragma unroll
+  for (int k = 0; k < D; k++) fx[(size_t)pid * D + k] = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
+  ft[pid] = a.meta[gi] & 0xff;
+}
+
+// reference cell ids floor(x / cl) (pyrdsim.pyx:1506-1508) of one system
+template <int D>
+__global__ void k_ref_cells(const SysDev* sysv, int sys, Args a, const double* cl, int p0, int n,
+                            int pid0, int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SysDev& s = sysv[sys];
+  const int gi = p0 + i;
+  const int pid = a.pid[gi] - pid0;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    double x = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
+    out[(size_t)pid * D + k] = (int)floor(__ddiv_rn(x, cl[k]));
+  }
+}
+
+// neighbour list as the reference would rebuild it now (pyrdsim.pyx:1448-1587):
+// bonded-list pairs plus partner-type pairs of different molecules, d <= rs.
+template <int D>
+__global__ void k_pairs(const SysDev* sysv, int sys, Args a, const TmplDev* tmpl, double rs,
+                        float rs2_hi, int p0, int n, int pid0, int* out, unsigned long long cap,
+                        unsigned long long* count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SysDev& s = sysv[sys];
+  const int gi = p0 + i;
+  const uint32_t mi = a.meta[gi];
+  const int pi = a.pid[gi] - pid0;
+  const int ti = mi & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
+  const uint32_t bmask = tmi != 0xff ? tmpl[tmi].bondmask[loci] : 0u;
+  for (int j = 0; j < n; j++) {
+    const int gj = p0 + j;
+    const int pj = a.pid[gj] - pid0;
+    if (pj <= pi) continue;
+    const uint32_t mj = a.meta[gj];
+    bool listed;
+    if (a.mol[gj] == a.mol[gi]) listed = (bmask >> ((mj >> 16) & 31)) & 1;
+    else listed = (s.partner[ti] >> (mj & 0xff)) & 1;
+    if (!listed) continue;
+    float r2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      float dx = (float)(int)(a.xh[k][gj] - a.xh[k][gi]) * s.unit_hi[k];
+      r2 += dx * dx;
+    }
+    if (r2 > rs2_hi) continue;
+    if (exact_dist<D>(s, a, gi, gj) > rs) continue;
+    unsigned long long slot = atomicAdd(count, 1ull);
+    if (slot < cap) {
+      out[2 * slot] = pi;
+      out[2 * slot + 1] = pj;
+    }
+  }
+}
+
+}  // namespace rd

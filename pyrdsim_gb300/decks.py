@@ -236,6 +236,77 @@ def load_initial_conditions(filename, n_dim, n_species,
             np.array(first_index, dtype=np.int32))
 
 
+def write_decks(directory, parameters, x, particle_types, molecule_ids,
+                molecule_parameters=None, molecule_interactions=None):
+    """Write a system given in dictionary form as the four deck files plus
+    ``initial_conditions.txt`` (default names) in the reference's grammar."""
+    import os
+    p = parameters
+
+    def arr(v):
+        return " ".join(repr(float(e)) for e in np.atleast_1d(v))
+
+    lines = [f"N_dim = {int(p['n_dim'])}", f"L = {arr(p['l'])}",
+             "periodic = " + " ".join(str(int(np.sign(v))) for v in np.atleast_1d(p["periodic"])),
+             f"dt = {float(p['dt'])!r}", f"N_steps = {int(p['n_steps'])}",
+             f"stride = {int(p.get('stride', 1))}", f"N_out = {int(p['n_out'])}",
+             f"tau_by_tauD = {arr(p.get('tau_by_taud', [1.0]))}"]
+    for key in ("rs",):
+        if key in p:
+            lines.append(f"{key} = {float(p[key])!r}")
+    for key in ("neighbor_list_update_frequency", "cell_length_ratio"):
+        if key in p:
+            lines.append(f"{key} = {int(p[key])}")
+    with open(os.path.join(directory, "parameters.txt"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    with open(os.path.join(directory, "nonbonded_interactions.txt"), "w") as f:
+        for it in p.get("interactions", []):
+            f.write("[ interaction ]\n")
+            for k, v in it.items():
+                if k == "pair":
+                    f.write("pair = " + " ".join(str(int(e)) for e in v) + "\n")
+                elif isinstance(v, str):
+                    f.write(f"{k} = {v}\n")
+                elif isinstance(v, (int, np.integer)) and k in ("n", "particle_type", "direction"):
+                    f.write(f"{k} = {int(v)}\n")
+                else:
+                    f.write(f"{k} = {float(v)!r}\n")
+            f.write("\n")
+    with open(os.path.join(directory, "reactions.txt"), "w") as f:
+        for r in p.get("reactions", []):
+            f.write("[ reaction ]\n")
+            for k, v in r.items():
+                if isinstance(v, str):
+                    f.write(f"{k} = {v}\n")
+                elif k in ("rate", "r0", "rate_decrease"):
+                    f.write(f"{k} = {float(v)!r}\n")
+                else:
+                    f.write(f"{k} = {int(v)}\n")
+            f.write("\n")
+    mp = molecule_parameters if molecule_parameters is not None else \
+        {0: {"molecule_id": 0, "n_atoms": 1}}
+    mi = molecule_interactions if molecule_interactions is not None else {0: []}
+    with open(os.path.join(directory, "bonded_interactions.txt"), "w") as f:
+        for mid, prm in mp.items():
+            f.write(f"[ molecule ]\nmolecule_id = {int(mid)}\nN_atoms = {int(prm['n_atoms'])}\n")
+            f.write("[ bonds ]\n")
+            for t in mi.get(mid, []):
+                if t["type"] == "bond":
+                    i, j = t["participants"]
+                    f.write(f"{i} {j} {float(t['r0'])!r} {float(t['u0'])!r}\n")
+            f.write("[ angles ]\n")
+            for t in mi.get(mid, []):
+                if t["type"] == "angle":
+                    i, j, k = t["participants"]
+                    f.write(f"{i} {j} {k} {float(t['theta0']) * 180.0 / np.pi!r} "
+                            f"{float(t['u0']) / (180.0 / np.pi) ** 2!r}\n")
+            f.write("\n")
+    with open(os.path.join(directory, "initial_conditions.txt"), "w") as f:
+        for i in range(len(x)):
+            f.write(" ".join(str(int(v)) for v in molecule_ids[i]) + f" {int(particle_types[i])} "
+                    + " ".join(repr(float(v)) for v in x[i]) + "\n")
+
+
 def write_state(filename, x, particle_types, molecule_ids):
     """pyrdsim.pyx:1917-1934 (``write_current_state_to_text_file``)."""
     n, d = x.shape

@@ -1,0 +1,215 @@
+"""ctypes binding of the GPU engine (``_lib/librdsim.so``, C ABI in
+``include/rdsim.h``).
+
+There is no CPU fallback: if the library cannot be loaded or no CUDA device
+is present, constructing an :class:`Engine` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "librdsim.so")
+_lib = None
+
+EXPORTS = [
+    "rdsim_create", "rdsim_destroy", "rdsim_step", "rdsim_set_state", "rdsim_get_state",
+    "rdsim_get_drift", "rdsim_get_reaction_rates", "rdsim_get_pairs", "rdsim_get_cell_ids",
+    "rdsim_get_step", "rdsim_set_step", "rdsim_set_trajectory", "rdsim_get_trajectory",
+    "rdsim_get_error", "rdsim_get_stream", "rdsim_get_info", "rdsim_last_error",
+    "rdsim_set_profiling", "rdsim_get_profile",
+]
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+def load_library(path=None):
+    """Load librdsim.so and declare the signatures of every export."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"GPU engine library not built: {p} "
+                          "(run `python -c 'import __graft_entry__ as g; g.build()'`)")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int32)
+    L.rdsim_create.argtypes = [C.POINTER(abi.System), C.c_int32, C.POINTER(abi.Options),
+                               C.POINTER(vp)]
+    L.rdsim_destroy.argtypes = [vp]
+    L.rdsim_step.argtypes = [vp, C.c_int32, C.c_int32, dp, dp, dp]
+    L.rdsim_set_state.argtypes = [vp, dp, ip]
+    L.rdsim_get_state.argtypes = [vp, dp, ip]
+    L.rdsim_get_drift.argtypes = [vp, dp]
+    L.rdsim_get_reaction_rates.argtypes = [vp, dp]
+    L.rdsim_get_pairs.argtypes = [vp, C.c_int32, ip, C.c_int64, C.POINTER(C.c_int64)]
+    L.rdsim_get_cell_ids.argtypes = [vp, C.c_int32, ip]
+    L.rdsim_get_step.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.rdsim_set_step.argtypes = [vp, C.c_int64]
+    L.rdsim_set_trajectory.argtypes = [vp, C.c_int32, C.c_int32]
+    L.rdsim_get_trajectory.argtypes = [vp, dp, ip]
+    L.rdsim_get_error.argtypes = [vp, ip, C.POINTER(C.c_int64), ip, dp, C.POINTER(C.c_int64)]
+    L.rdsim_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.rdsim_get_info.argtypes = [vp, C.POINTER(abi.Info)]
+    L.rdsim_set_profiling.argtypes = [vp, C.c_int32]
+    L.rdsim_get_profile.argtypes = [vp, C.POINTER(abi.Profile)]
+    L.rdsim_last_error.restype = C.c_char_p
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        msg = load_library().rdsim_last_error().decode()
+        if rc == abi.ERR_OUT_OF_BOUNDS:
+            raise EngineError(rc, msg)
+        raise EngineError(rc, msg)
+
+
+class Engine:
+    """A batch of systems stepped together on one GPU.
+
+    ``systems`` is a list of :class:`pyrdsim_gb300.model.SystemData`.  Particle
+    arrays at this interface are in the caller's order, systems concatenated.
+    """
+
+    def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, tile_target=0):
+        self.lib = load_library()
+        self.systems = list(systems)
+        self.D = self.systems[0].model.N_dim
+        self.offsets = np.cumsum([0] + [s.n_particles for s in self.systems])
+        self.N = int(self.offsets[-1])
+        arr = (abi.System * len(self.systems))(*[s.struct for s in self.systems])
+        opt = abi.Options()
+        opt.device = device
+        opt.skin = skin
+        opt.threads_per_particle = threads_per_particle
+        opt.tile_target = tile_target
+        h = C.c_void_p()
+        _check(self.lib.rdsim_create(arr, len(self.systems), C.byref(opt), C.byref(h)))
+        self.h = h
+        self._traj = (0, 0)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rdsim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- stepping ------------------------------------------------------
+    def step(self, n, xi=None, u1=None, u2=None, noise=True, device_arrays=False):
+        """Advance ``n`` steps.  With ``xi`` (n, N, D) and ``u1``/``u2`` (n, N)
+        the noise is injected, otherwise counter-based Philox is used."""
+        flags = 0 if noise else abi.STEP_NO_NOISE
+        if xi is not None or u1 is not None:
+            if device_arrays:
+                flags |= abi.STEP_INJECT_DEVICE
+                _check(self.lib.rdsim_step(self.h, int(n), flags,
+                                           C.cast(C.c_void_p(xi), C.POINTER(C.c_double)),
+                                           C.cast(C.c_void_p(u1), C.POINTER(C.c_double)),
+                                           C.cast(C.c_void_p(u2), C.POINTER(C.c_double))))
+                return
+            flags |= abi.STEP_INJECT_HOST
+            xi = None if xi is None else np.ascontiguousarray(xi, dtype=np.float64)
+            u1 = None if u1 is None else np.ascontiguousarray(u1, dtype=np.float64)
+            u2 = None if u2 is None else np.ascontiguousarray(u2, dtype=np.float64)
+            _check(self.lib.rdsim_step(self.h, int(n), flags, abi.dptr(xi), abi.dptr(u1),
+                                       abi.dptr(u2)))
+        else:
+            _check(self.lib.rdsim_step(self.h, int(n), flags, None, None, None))
+
+    def set_state(self, x=None, types=None):
+        x = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
+        _check(self.lib.rdsim_set_state(self.h, abi.dptr(x), abi.iptr(t)))
+
+    def state(self):
+        x = np.empty((self.N, self.D))
+        t = np.empty(self.N, dtype=np.int32)
+        _check(self.lib.rdsim_get_state(self.h, abi.dptr(x), abi.iptr(t)))
+        return x, t
+
+    def drift(self):
+        a = np.empty((self.N, self.D))
+        _check(self.lib.rdsim_get_drift(self.h, abi.dptr(a)))
+        return a
+
+    def reaction_rates(self):
+        r = np.empty(self.N)
+        _check(self.lib.rdsim_get_reaction_rates(self.h, abi.dptr(r)))
+        return r
+
+    def pairs(self, sys=0):
+        n = C.c_int64()
+        rc = self.lib.rdsim_get_pairs(self.h, sys, None, 0, C.byref(n))
+        if rc not in (0, abi.ERR_CAPACITY):
+            _check(rc)
+        out = np.empty((max(1, n.value), 2), dtype=np.int32)
+        _check(self.lib.rdsim_get_pairs(self.h, sys, abi.iptr(out), n.value, C.byref(n)))
+        return out[: n.value]
+
+    def cell_ids(self, sys=0):
+        n = self.systems[sys].n_particles
+        c = np.empty((n, self.D), dtype=np.int32)
+        _check(self.lib.rdsim_get_cell_ids(self.h, sys, abi.iptr(c)))
+        return c
+
+    @property
+    def step_index(self):
+        s = C.c_int64()
+        _check(self.lib.rdsim_get_step(self.h, C.byref(s)))
+        return s.value
+
+    @step_index.setter
+    def step_index(self, v):
+        _check(self.lib.rdsim_set_step(self.h, int(v)))
+
+    def set_trajectory(self, stride, n_frames):
+        _check(self.lib.rdsim_set_trajectory(self.h, int(stride), int(n_frames)))
+        self._traj = (int(stride), int(n_frames))
+
+    def trajectory(self):
+        _, nf = self._traj
+        x = np.zeros((nf, self.N, self.D))
+        t = np.zeros((nf, self.N), dtype=np.int32)
+        if nf:
+            _check(self.lib.rdsim_get_trajectory(self.h, abi.dptr(x), abi.iptr(t)))
+        return x, t
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(self.lib.rdsim_get_stream(self.h, C.byref(s)))
+        return s.value
+
+    def set_profiling(self, on=True):
+        _check(self.lib.rdsim_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self):
+        """Launch counts and event-timed device ms per kernel class since the
+        last call (resets the counters)."""
+        p = abi.Profile()
+        _check(self.lib.rdsim_get_profile(self.h, C.byref(p)))
+        return {name: {"launches": p.launches[c], "ms": p.ms[c], "timed": p.timed[c]}
+                for c, name in enumerate(abi.PROFILE_NAMES)}
+
+    def info(self):
+        i = abi.Info()
+        _check(self.lib.rdsim_get_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in abi.Info._fields_}

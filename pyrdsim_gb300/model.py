@@ -22,8 +22,9 @@ from . import abi, decks
 class Model:
     """Parsed, validated parameters of one system (no particle state)."""
 
-    def __init__(self, parameters=None):
+    def __init__(self, parameters=None, _bonded=None):
         parameters = {} if parameters is None else parameters
+        self._bonded = _bonded
         # pyrdsim.pyx:307-334 defaults
         self.parameters_filename = "parameters.txt"
         self.bint_filename = "./bonded_interactions.txt"
@@ -43,6 +44,8 @@ class Model:
         if "parameters_filename" in parameters:
             self.parameters_filename = parameters["parameters_filename"]
         try:
+            if _bonded is not None:
+                raise FileNotFoundError  # dictionary-only construction
             loaded = decks.load_parameters_file(
                 self.parameters_filename, decks.PARAMETERS_DATATYPES,
                 decks.PARAMETERS_INT_ARRAYS, decks.PARAMETERS_FLOAT_ARRAYS,
@@ -56,6 +59,7 @@ class Model:
 
     # pyrdsim.pyx:406-587
     def set_parameters(self, p):
+        self.parameters = dict(p)
         if "comment_chars" in p:
             self.comment_chars = p["comment_chars"]
         seed = p.get("seed", -1)
@@ -131,8 +135,11 @@ class Model:
                 self._add_pair(int(r["reactant"]), int(r["inhibitor"]))
                 if "inhibitor2" in r:
                     self._add_pair(int(r["reactant"]), int(r["inhibitor2"]))
-        self.molecule_parameters, self.molecule_interactions = \
-            decks.load_bonded_interactions(self.bint_filename, cc)
+        if self._bonded is not None:
+            self.molecule_parameters, self.molecule_interactions = self._bonded
+        else:
+            self.molecule_parameters, self.molecule_interactions = \
+                decks.load_bonded_interactions(self.bint_filename, cc)
         if "cell_length_ratio" in p:
             self.cell_length_ratio = int(p["cell_length_ratio"])
         if "rs" in p:
@@ -143,6 +150,19 @@ class Model:
             self.neighbor_list_update_frequency = int(p["neighbor_list_update_frequency"])
         # GPU-only options live in their own namespace (keys starting "gpu_")
         self.gpu_options = {k: v for k, v in p.items() if str(k).startswith("gpu_")}
+
+    @classmethod
+    def from_dict(cls, parameters, molecule_parameters=None, molecule_interactions=None):
+        """Build from a parameter dictionary alone (no deck files are read).
+
+        ``parameters`` must hold ``interactions`` and ``reactions`` lists;
+        molecules default to one single-atom molecule type with id 0."""
+        mp = molecule_parameters if molecule_parameters is not None else \
+            {0: {"molecule_id": 0, "n_atoms": 1}}
+        mi = molecule_interactions if molecule_interactions is not None else {0: []}
+        p = dict(parameters)
+        p.setdefault("reactions", [])
+        return cls(p, _bonded=(mp, mi))
 
     def _add_pair(self, i0, i1):  # pyrdsim.pyx:1234-1263
         self.interaction_partners.setdefault(i0, set()).add(i1)

@@ -1,0 +1,179 @@
+"""Seeded synthetic systems with the shapes of the benchmark configurations.
+
+Each builder returns a :class:`pyrdsim_gb300.model.SystemData` (parameters in
+the reference's dictionary form plus an initial state).  Positions start on a
+jittered square lattice at the target density: uniform random placement would
+overlap Lennard-Jones cores and blow the first step up, while a lattice with
+jitter below half the spacing keeps every pair beyond 0.9 sigma.
+
+* ``lj_fluid``          -- 2D single-species LJ, periodic (N=1024, rho=0.5)
+* ``active_wall_fluid`` -- 2D two-species WCA/LJ with a 9-3 wall and
+                           activation / catalysed deactivation (N=65,536,
+                           rho=0.4, periodic x, reflecting y)
+* ``patchy_colloids``   -- 2D three-patch colloids, 16,384 molecules x 4
+* ``ensemble``          -- 512 independent systems of uneven size
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import model
+
+WCA_R0 = 2.0 ** (1.0 / 6.0)
+
+
+def jittered_lattice(n, L, rng, jitter=0.25):
+    """n points on a jittered square lattice filling an L[0] x L[1] box."""
+    L = np.asarray(L, float)
+    nx = int(np.ceil(np.sqrt(n * L[0] / L[1])))
+    ny = int(np.ceil(n / nx))
+    sx, sy = L[0] / nx, L[1] / ny
+    ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    pts = np.stack([(ix.reshape(-1) + 0.5) * sx, (iy.reshape(-1) + 0.5) * sy], 1)
+    pts = pts[rng.permutation(len(pts))[:n]]
+    pts += rng.uniform(-jitter, jitter, pts.shape) * np.array([sx, sy])
+    return pts
+
+
+def _single_atoms(n):
+    mol = np.stack([np.arange(n), np.zeros(n, int), np.zeros(n, int)], 1).astype(np.int32)
+    return mol, np.arange(n, dtype=np.int32)
+
+
+def lj_fluid(n=1024, rho=0.5, seed=1, dt=1e-4):
+    rng = np.random.default_rng(seed)
+    L = np.sqrt(n / rho)
+    params = {
+        "n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, 1.0]),
+        "dt": dt, "n_steps": 10000, "n_out": 100000, "tau_by_taud": np.array([1.0]),
+        "seed": seed,
+        "interactions": [{"type": "lj", "pair": [0, 0], "u0": 1.0, "r0": WCA_R0,
+                          "rc": 2.5, "n": 6}],
+        "reactions": [],
+    }
+    m = model.Model.from_dict(params)
+    x = jittered_lattice(n, [L, L], rng)
+    mol, first = _single_atoms(n)
+    return model.SystemData(m, x, np.zeros(n, np.int32), mol, first)
+
+
+def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93"):
+    """Two species: 0 inactive (WCA only), 1 active (LJ among actives, 9-3 wall).
+
+    Reactions: activation 0 -> 1 at rate 0.1; deactivation 1 -> 0 at rate 1.0
+    per active neighbour within 1.5 sigma.  ``wall="wall"`` swaps the 9-3 wall
+    for the reference's tanh wall (for running the same shape in the reference).
+    """
+    rng = np.random.default_rng(seed)
+    L = np.sqrt(n / rho)
+    if wall == "wall93":
+        w = {"type": "wall93", "particle_type": 1, "direction": 1, "u0": 1.0, "r0": 1.0,
+             "rc": 2.5}
+    else:
+        w = {"type": "wall", "particle_type": 1, "direction": 1, "u0": 1.0, "r0": 1.0,
+             "a": 0.5, "rc": 2.5}
+    params = {
+        "n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, -1.0]),
+        "dt": dt, "n_steps": 20000, "n_out": 1000000, "tau_by_taud": np.array([1.0, 1.0]),
+        "seed": seed,
+        "interactions": [
+            {"type": "lj", "pair": [0, 0], "u0": 1.0, "r0": WCA_R0, "rc": WCA_R0, "n": 6},
+            {"type": "lj", "pair": [0, 1], "u0": 1.0, "r0": WCA_R0, "rc": WCA_R0, "n": 6},
+            {"type": "lj", "pair": [1, 1], "u0": 1.0, "r0": WCA_R0, "rc": 2.5, "n": 6},
+            w,
+        ],
+        "reactions": [
+            {"type": "linear", "reactant": 0, "product": 1, "rate": 0.1},
+            {"type": "locally_catalyzed", "reactant": 1, "catalyst": 1, "product": 0,
+             "rate": 1.0, "r0": 1.5},
+        ],
+    }
+    m = model.Model.from_dict(params)
+    x = jittered_lattice(n, [L, L], rng)
+    types = rng.integers(0, 2, n).astype(np.int32)
+    mol, first = _single_atoms(n)
+    return model.SystemData(m, x, types, mol, first)
+
+
+def patchy_colloids(n_molecules=16384, phi=0.3, seed=3, dt=1e-5):
+    """Three-patch colloids: core (type 0) + patches (1 inactive, 2 active)."""
+    rng = np.random.default_rng(seed)
+    L = np.sqrt(n_molecules * np.pi / 4 / phi)
+    centres = jittered_lattice(n_molecules, [L, L], rng, jitter=0.1)
+    phi0 = rng.uniform(0, 2 * np.pi, n_molecules)
+    x = np.zeros((n_molecules, 4, 2))
+    x[:, 0] = centres
+    for q in range(3):
+        ang = phi0 + 2 * np.pi * q / 3
+        x[:, q + 1] = centres + 0.5 * np.stack([np.cos(ang), np.sin(ang)], 1)
+    x = x.reshape(-1, 2) % L
+    n = 4 * n_molecules
+    types = np.zeros((n_molecules, 4), np.int32)
+    types[:, 1:] = 1 + rng.integers(0, 2, (n_molecules, 3))
+    mol = np.zeros((n_molecules, 4, 3), np.int32)
+    mol[:, :, 0] = np.arange(n_molecules)[:, None]
+    mol[:, :, 1] = np.arange(4)[None, :]
+    params = {
+        "n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, 1.0]),
+        "dt": dt, "n_steps": 50000, "n_out": 1000000,
+        "tau_by_taud": np.array([1.0, 5.0, 5.0]), "seed": seed,
+        "interactions": [
+            {"type": "lj", "pair": [0, 0], "u0": 1.0, "r0": WCA_R0, "rc": WCA_R0, "n": 6},
+            {"type": "tanh", "pair": [2, 2], "u0": 5.0, "r0": 0.1, "a": 0.05, "rc": 0.4},
+        ],
+        "reactions": [
+            {"type": "linear", "reactant": 1, "product": 2, "rate": 1.0},
+            {"type": "locally_catalyzed", "reactant": 2, "catalyst": 2, "product": 1,
+             "rate": 5.0, "r0": 0.25},
+        ],
+    }
+    bonds = []
+    for i, j, r0 in [(0, 1, 0.5), (0, 2, 0.5), (0, 3, 0.5),
+                     (1, 2, 0.866), (2, 3, 0.866), (3, 1, 0.866)]:
+        bonds.append({"type": "bond", "participants": [i, j], "r0": r0, "u0": 500.0})
+    m = model.Model.from_dict(params, {0: {"molecule_id": 0, "n_atoms": 4}}, {0: bonds})
+    first = np.arange(0, n, 4, dtype=np.int32)
+    return model.SystemData(m, x, types.reshape(-1), mol.reshape(-1, 3), first)
+
+
+def ensemble(n_systems=512, seed=4, dt=1e-4, n_min=256, n_max=16384):
+    """Independent systems: N log-uniform, density U[0.2, 0.7], kT U[0.5, 2],
+    LJ or Yukawa (p = 1/2), half with two-state linear reactions.  Energies
+    are in units of kT and D = kT (friction 1)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_systems):
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        rho = rng.uniform(0.2, 0.7)
+        kT = rng.uniform(0.5, 2.0)
+        L = np.sqrt(n / rho)
+        if rng.random() < 0.5:
+            inter = {"type": "lj", "r0": WCA_R0, "rc": 2.5, "n": 6, "u0": 1.0 / kT}
+        else:
+            inter = {"type": "yukawa", "r0": 1.0, "rc": 5.0, "u0": 10.0 / kT}
+        react = rng.random() < 0.5
+        ntypes = 2 if react else 1
+        inters = []
+        for a in range(ntypes):
+            for b in range(a, ntypes):
+                d = dict(inter)
+                d["pair"] = [a, b]
+                inters.append(d)
+        reactions = []
+        if react:
+            reactions = [
+                {"type": "linear", "reactant": 0, "product": 1, "rate": rng.uniform(0.01, 1)},
+                {"type": "linear", "reactant": 1, "product": 0, "rate": rng.uniform(0.01, 1)},
+            ]
+        params = {
+            "n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, 1.0]),
+            "dt": dt, "n_steps": 5000, "n_out": 1000000,
+            "tau_by_taud": np.full(ntypes, kT), "seed": int(rng.integers(1, 2**31)),
+            "interactions": inters, "reactions": reactions,
+        }
+        m = model.Model.from_dict(params)
+        x = jittered_lattice(n, [L, L], rng)
+        types = rng.integers(0, ntypes, n).astype(np.int32)
+        mol, first = _single_atoms(n)
+        out.append(model.SystemData(m, x, types, mol, first))
+    return out

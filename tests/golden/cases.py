@@ -140,7 +140,8 @@ def case_patchy():
         xs.append(c); types.append(0); mol.append(m); local.append(0)
         for q in range(3):
             ang = phi + 2 * np.pi * q / 3
-            xs.append(c + 0.5 * np.array([np.cos(ang), np.sin(ang)]))
+            xs.append(c + 0.5 * np.array([np.cos(ang), np.sin(ang)])
+                      + rng.uniform(-0.02, 0.02, 2))
             types.append(1 + (q + m) % 2); mol.append(m); local.append(q + 1)
     x = np.array(xs)
     bonded = """[ molecule ]
@@ -178,20 +179,20 @@ rc=0.4
 """
     rx = """[ reaction ]
 type = linear
-rate=20.
+rate=300.
 reactant=1
 product=2
 
 [ reaction ]
 type = locally_catalyzed
-rate=40.
+rate=600.
 r0= 1.2
 reactant=2
 catalyst=2
 product=1
 """
     return dict(name="patchy",
-                parameters=_params(2, [9.3, 9.3], [1, 1], 1e-4, 40, [1.0, 5.0, 5.0], rs=2.5),
+                parameters=_params(2, [9.3, 9.3], [1, 1], 1e-5, 40, [1.0, 5.0, 5.0], rs=2.5),
                 nonbonded=nb, reactions=rx, bonded=bonded,
                 ic=_ic_text(x, np.array(types), np.array(mol), np.array(local),
                             np.zeros(len(x), int)), seed=13, steps=40)
@@ -225,7 +226,7 @@ dr = 0.5
 type = lj
 pair = 2 2
 U0 = 0.8
-r0 = 2.0
+r0 = 1.6
 rc = 3.5
 n = 10
 
@@ -239,8 +240,8 @@ rc = 3.0
 type = locally_inhibited
 reactant = 0
 product = 2
-rate = 30.
-rate_decrease = 10.
+rate = 300.
+rate_decrease = 100.
 inhibitor = 1
 inhibitor2 = 2
 r0 = 2.5
@@ -249,18 +250,18 @@ r0 = 2.5
 type = linear
 reactant = 2
 product = 0
-rate = 20.
+rate = 200.
 
 [ reaction ]
 type = locally_catalyzed
 reactant = 1
 catalyst = 0
 product = 0
-rate = 15.
+rate = 150.
 r0 = 2.0
 """
     return dict(name="mixed_laws",
-                parameters=_params(2, [14.4, 14.4], [1, 1], 1e-3, 40, [1.0, 0.5, 2.0], freq=7),
+                parameters=_params(2, [14.4, 14.4], [1, 1], 1e-4, 40, [1.0, 0.5, 2.0], freq=7),
                 nonbonded=nb, reactions=rx, bonded=SIMPLE_BONDED,
                 ic=_ic_text(x, types), seed=17, steps=40)
 

@@ -1,0 +1,163 @@
+"""GPU engine vs the CPU oracle on identical inputs (injected noise/uniforms).
+
+Bars (from the benchmark spec of this path):
+  * cell assignments, neighbour pair sets, reaction propensities and reaction
+    outcomes: bit-exact;
+  * per-step drift (forces): within 1e-5 relative of float64, norm-wise
+    (||a_gpu - a_ref|| / ||a_ref||) and per particle with a floor of the
+    RMS drift;
+  * positions after 100 steps: within 1e-6 relative (|dx| <= 1e-6 max(|x|, 1)).
+The oracle runs without the neighbour-history quirk of pyrdsim.pyx:1513
+(the GPU rebuilds its list from the current types).
+"""
+import numpy as np
+import pytest
+
+from helpers import CASE_NAMES, deck_dict, load_fixture, pair_set, system_from_deck
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-5
+POS_RTOL = 1e-6
+
+
+def _engine(sds, **kw):
+    from pyrdsim_gb300.engine import Engine
+    return Engine(sds, **kw)
+
+
+def _oracle(sd):
+    from oracle.oracle import Oracle
+    return Oracle(sd, history_quirk=False)
+
+
+def drift_errors(a, ref):
+    d = a - ref
+    norm = np.linalg.norm(d) / max(np.linalg.norm(ref), 1e-300)
+    mag = np.linalg.norm(ref, axis=1)
+    floor = max(np.sqrt(np.mean(mag ** 2)), 1e-300)
+    per = (np.linalg.norm(d, axis=1) / np.maximum(mag, floor)).max()
+    return norm, per
+
+
+def min_image(d, sd):
+    m = sd.model
+    d = d.copy()
+    for k in range(m.N_dim):
+        if m.periodic[k] > 0:
+            d[:, k] -= m.L[k] * np.round(d[:, k] / m.L[k])
+    return d
+
+
+def _case(name):
+    fx = load_fixture(name)
+    return fx, system_from_deck(deck_dict(fx), int(fx["seed"]))
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_setup_cells_pairs_drift_rates(name):
+    fx, sd = _case(name)
+    eng = _engine([sd])
+    orc = _oracle(sd)
+    np.testing.assert_array_equal(eng.cell_ids(), orc.cell_ids())
+    assert pair_set(eng.pairs()) == pair_set(orc.pairs())
+    norm, per = drift_errors(eng.drift(), orc.drift())
+    assert norm <= FORCE_RTOL and per <= FORCE_RTOL, (norm, per)
+    np.testing.assert_array_equal(eng.reaction_rates(), orc.reaction_rates(recompute=True))
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_100_steps_injected_noise(name):
+    fx, sd = _case(name)
+    n, D = sd.n_particles, sd.model.N_dim
+    rng = np.random.default_rng(1234)
+    steps = 100
+    xi = rng.standard_normal((steps, n, D))
+    u1 = rng.random((steps, n))
+    u2 = rng.random((steps, n))
+    eng = _engine([sd])
+    orc = _oracle(sd)
+    # ten calls of ten steps: exercises the call boundary (stand-alone EM)
+    for c in range(10):
+        sl = slice(10 * c, 10 * (c + 1))
+        eng.step(10, xi=xi[sl], u1=u1[sl], u2=u2[sl])
+        orc.step(10, xi=xi[sl], u1=u1[sl], u2=u2[sl])
+    xg, tg = eng.state()
+    xo, to = orc.state()
+    d = min_image(xg - xo, sd)
+    assert (np.abs(d) <= POS_RTOL * np.maximum(np.abs(xo), 1.0)).all(), np.abs(d).max()
+    np.testing.assert_array_equal(tg, to)
+    norm, per = drift_errors(eng.drift(), orc.drift())
+    assert norm <= FORCE_RTOL, (norm, per)
+    # identical state -> identical list and rates at this rebuild-free step
+    eng.set_state(xo, to)
+    orc.set_state(xo, to)
+    assert pair_set(eng.pairs()) == pair_set(orc.pairs())
+    norm, per = drift_errors(eng.drift(), orc.drift())
+    assert norm <= FORCE_RTOL and per <= FORCE_RTOL, (norm, per)
+
+
+def test_batched_equals_individual():
+    # 2D decks sharing neighbor_list_update_frequency = 10
+    names = ["lj_periodic", "two_species_wall_rx", "patchy", "angle_pi"]
+    sds = [_case(nm)[1] for nm in names]
+    batch = _engine(sds)
+    ab = batch.drift()
+    off = 0
+    for sd in sds:
+        e = _engine([sd])
+        np.testing.assert_array_equal(ab[off:off + sd.n_particles], e.drift())
+        off += sd.n_particles
+    rng = np.random.default_rng(7)
+    N = batch.N
+    xi = rng.standard_normal((20, N, 2))
+    u1 = rng.random((20, N))
+    u2 = rng.random((20, N))
+    batch.step(20, xi=xi, u1=u1, u2=u2)
+    xb, tb = batch.state()
+    off = 0
+    for sd in sds:
+        e = _engine([sd])
+        n = sd.n_particles
+        e.step(20, xi=xi[:, off:off + n], u1=u1[:, off:off + n], u2=u2[:, off:off + n])
+        xe, te = e.state()
+        np.testing.assert_array_equal(xb[off:off + n], xe)
+        np.testing.assert_array_equal(tb[off:off + n], te)
+        off += n
+
+
+def test_out_of_bounds_raises_like_reference():
+    fx, sd = _case("two_species_wall_rx")
+    eng = _engine([sd])
+    n = sd.n_particles
+    xi = np.zeros((1, n, 2))
+    xi[0, 3, 1] = 1e6   # a displacement far beyond the reflecting box
+    with pytest.raises(RuntimeError):
+        eng.step(1, xi=xi, u1=np.ones((1, n)), u2=np.ones((1, n)))
+
+
+def test_philox_noise_statistics():
+    """Free particles: displacement variance 2 D dt per step and dimension."""
+    from pyrdsim_gb300 import model
+    n = 20000
+    rng = np.random.default_rng(3)
+    L = 1000.0
+    x = rng.uniform(0, L, (n, 2))
+    params = {"n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, 1.0]),
+              "dt": 1e-2, "n_steps": 1, "n_out": 10, "tau_by_taud": np.array([0.5]),
+              "seed": 9, "interactions": [], "reactions": [], "rs": 1.0}
+    m = model.Model.from_dict(params)
+    mol = np.stack([np.arange(n), np.zeros(n, int), np.zeros(n, int)], 1).astype(np.int32)
+    sd = model.SystemData(m, x, np.zeros(n, np.int32), mol, np.arange(n, dtype=np.int32))
+    eng = _engine([sd])
+    eng.step(4)
+    x1, _ = eng.state()
+    d = min_image(x1 - x, sd)
+    var = d.var(axis=0)
+    expect = 4 * 2 * 0.5 * 1e-2
+    assert np.all(np.abs(var / expect - 1) < 0.05), var / expect
+    assert np.abs(d.mean(axis=0)).max() < 5 * np.sqrt(expect / n)
+    # same seed -> identical run; different seed -> different run
+    eng2 = _engine([sd])
+    eng2.step(4)
+    np.testing.assert_array_equal(eng2.state()[0], x1)
