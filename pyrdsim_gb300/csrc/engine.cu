@@ -394,7 +394,8 @@ int upload_state(rdsim_handle* h, const std::vector<double>& x, const std::vecto
         double v = x[(size_t)g * D + k];
         bool per = (q.periodic_mask >> k) & 1;
         if (!per) {
-          if (!(v >= -q.L[k] && v <= 1.999 * q.L[k]))
+          // int64 fixed point holds [-L, L] (L maps to 2^63 - 2^34)
+          if (!(v >= -q.L[k] && v <= q.L[k] * (1.0 + 1e-9)))
             return fail(RDSIM_ERR_ARG, "initial position outside the reflecting box");
         } else if (!std::isfinite(v)) {
           return fail(RDSIM_ERR_ARG, "non-finite initial position");

@@ -355,16 +355,20 @@ __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid
     if ((s.periodic >> k) & 1) {
       X += (unsigned long long)d;
     } else {
-      long long Xs = (long long)X + d;
-      long long Si = s.Si[k];
+      // reflect (pyrdsim.pyx:2275-2280) in 128-bit arithmetic: 2*S overflows int64
+      __int128 Xs = (__int128)(long long)X + d;
+      const __int128 Si = s.Si[k];
       if (Xs > Si) Xs = 2 * Si - Xs;
       if (Xs < 0) Xs = -Xs;
       if (Xs < 0 || Xs > Si) {
         record_error(a.err, RDSIM_ERR_OUT_OF_BOUNDS, pid, k,
-                     __dmul_rn(__ll2double_rn(Xs), s.unit_d[k]), em_step);
+                     __dmul_rn(__ll2double_rn((long long)(Xs > Si ? Si : 0)), s.unit_d[k]) +
+                         __dmul_rn(__ll2double_rn((long long)(Xs > Si ? Xs - Si : Xs)),
+                                   s.unit_d[k]),
+                     em_step);
         Xs = Xs < 0 ? 0 : Si;
       }
-      X = (unsigned long long)Xs;
+      X = (unsigned long long)(long long)Xs;
     }
     a.xh_out[k][gi] = (uint32_t)(X >> 32);
     a.xl_out[k][gi] = (uint32_t)X;
@@ -723,6 +727,9 @@ __global__ void k_bin(const SysDev* sysv, const int* sid, const uint32_t* x0, co
 #pragma unroll
     for (int k = 0; k < D; k++) {
       unsigned long long h = xs[k][i];
+      // reflecting dimensions hold signed values (an initial position may lie
+      // below 0 until the first boundary step)
+      if (!((s.periodic >> k) & 1) && (int)xs[k][i] < 0) h = 0;
       int c = (int)((h * (unsigned long long)s.nc[k]) / s.hrange[k]);
       if (c >= s.nc[k]) c = s.nc[k] - 1;
       if (c < 0) c = 0;

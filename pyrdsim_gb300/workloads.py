@@ -22,14 +22,17 @@ from . import model
 WCA_R0 = 2.0 ** (1.0 / 6.0)
 
 
-def jittered_lattice(n, L, rng, jitter=0.25):
-    """n points on a jittered square lattice filling an L[0] x L[1] box."""
+def jittered_lattice(n, L, rng, jitter=0.1, lo=(0.0, 0.0)):
+    """n points on a jittered square lattice filling [lo, L] (2D); the closest
+    pair is at least (1 - 2 jitter) lattice spacings apart."""
     L = np.asarray(L, float)
-    nx = int(np.ceil(np.sqrt(n * L[0] / L[1])))
+    lo = np.asarray(lo, float)
+    W = L - lo
+    nx = int(np.ceil(np.sqrt(n * W[0] / W[1])))
     ny = int(np.ceil(n / nx))
-    sx, sy = L[0] / nx, L[1] / ny
+    sx, sy = W[0] / nx, W[1] / ny
     ix, iy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
-    pts = np.stack([(ix.reshape(-1) + 0.5) * sx, (iy.reshape(-1) + 0.5) * sy], 1)
+    pts = np.stack([lo[0] + (ix.reshape(-1) + 0.5) * sx, lo[1] + (iy.reshape(-1) + 0.5) * sy], 1)
     pts = pts[rng.permutation(len(pts))[:n]]
     pts += rng.uniform(-jitter, jitter, pts.shape) * np.array([sx, sy])
     return pts
@@ -69,9 +72,16 @@ def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93"):
     if wall == "wall93":
         w = {"type": "wall93", "particle_type": 1, "direction": 1, "u0": 1.0, "r0": 1.0,
              "rc": 2.5}
+        # inactive particles get the repulsive part only (cut at the 9-3
+        # minimum, (2/5)^(1/6) sigma): without it an inactive particle can
+        # reach y ~ 0 and, once activated, meet the 1/y^10 core of the wall
+        w0 = {"type": "wall93", "particle_type": 0, "direction": 1, "u0": 1.0, "r0": 1.0,
+              "rc": 0.4 ** (1.0 / 6.0)}
     else:
         w = {"type": "wall", "particle_type": 1, "direction": 1, "u0": 1.0, "r0": 1.0,
              "a": 0.5, "rc": 2.5}
+        w0 = {"type": "wall", "particle_type": 0, "direction": 1, "u0": 1.0, "r0": 0.5,
+              "a": 0.25, "rc": 1.0}
     params = {
         "n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, -1.0]),
         "dt": dt, "n_steps": 20000, "n_out": 1000000, "tau_by_taud": np.array([1.0, 1.0]),
@@ -80,7 +90,7 @@ def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93"):
             {"type": "lj", "pair": [0, 0], "u0": 1.0, "r0": WCA_R0, "rc": WCA_R0, "n": 6},
             {"type": "lj", "pair": [0, 1], "u0": 1.0, "r0": WCA_R0, "rc": WCA_R0, "n": 6},
             {"type": "lj", "pair": [1, 1], "u0": 1.0, "r0": WCA_R0, "rc": 2.5, "n": 6},
-            w,
+            w, w0,
         ],
         "reactions": [
             {"type": "linear", "reactant": 0, "product": 1, "rate": 0.1},
@@ -89,7 +99,8 @@ def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93"):
         ],
     }
     m = model.Model.from_dict(params)
-    x = jittered_lattice(n, [L, L], rng)
+    # keep one sigma from the y = 0 wall (the 9-3 minimum is at 0.86 sigma)
+    x = jittered_lattice(n, [L, L - 0.5], rng, lo=(0.0, 1.0))
     types = rng.integers(0, 2, n).astype(np.int32)
     mol, first = _single_atoms(n)
     return model.SystemData(m, x, types, mol, first)
