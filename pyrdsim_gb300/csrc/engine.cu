@@ -933,7 +933,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     }
     int cap = (int)std::ceil(worst / 256.0) * 256;
     h->cap = std::max(512, std::min(4096, cap));
-    h->dyn_smem = (size_t)h->cap * (D + 3) * 4;
+    h->dyn_smem = (size_t)h->cap * (D + 4 + std::max(D, MAXR / 2)) * 4;
   }
   // device memory
   int64_t& B = h->device_bytes;

@@ -376,325 +376,374 @@ __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid
 }
 
 // ---------------------------------------------------------------------------
-// Drift kernel.
+// Drift kernel.  Phase A: TPP threads per own particle run the pair loop and
+// combine with shuffles into shared memory.  Phase B: one thread per own
+// particle adds walls and bonded terms, stores the drift and/or performs the
+// fused Euler-Maruyama update, so no lane idles in the per-particle tail.
 template <int D, int TPP>
-__global__ void __launch_bounds__(BLOCK) k_force(Args a) {
+__global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
   extern __shared__ uint32_t dyn[];
   __shared__ TileShared<D> sh;
   const Tile t = a.tiles[blockIdx.x];
   Staged<D> st = tile_setup<D>(sh, a, t, dyn);
   const SysDev& s = sh.sys;
+  int* oidx = reinterpret_cast<int*>(dyn + (D + 3) * a.cap);
+  float* ofr = reinterpret_cast<float*>(dyn + (D + 4) * a.cap);
   const int tid = threadIdx.x;
   const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
   const int nhc = sh.nhc, nown = sh.nown;
-  for (int p0 = 0; p0 < nown; p0 += groups) {
-    const int p = p0 + g;
-    const bool active = p < nown;
-    float acc[3] = {0.f, 0.f, 0.f};
-    int q = 0, idx = 0, gi = 0;
-    uint32_t mi = 0;
-    if (active) {
-      q = last_le(sh.own, nhc, p);
-      idx = sh.beg[q] + (p - sh.own[q]);
-      gi = st.gi ? st.gi[idx] : idx;
-      uint32_t xi_h[3];
+  for (int base = 0; base < nown; base += a.cap) {
+    const int nch = min(a.cap, nown - base);
+    for (int p0 = 0; p0 < nch; p0 += groups) {
+      const int pl = p0 + g;
+      const bool active = pl < nch;
+      float acc[3] = {0.f, 0.f, 0.f};
+      int idx = 0;
+      if (active) {
+        const int p = base + pl;
+        const int q = last_le(sh.own, nhc, p);
+        idx = sh.beg[q] + (p - sh.own[q]);
+        const int gi = st.gi ? st.gi[idx] : idx;
+        uint32_t xi_h[3];
 #pragma unroll
-      for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
-      mi = st.meta[idx];
-      const int moli = st.mol[idx];
-      const int ti = mi & 0xff, trbi = (mi >> 8) & 0xff;
-      const unsigned int pmask = s.partner[trbi];
-      if (s.R2 > 0.f) for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
-        float dx[3], r2 = 0.f;
+        for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
+        const uint32_t mi = st.meta[idx];
+        const int moli = st.mol[idx];
+        const int ti = mi & 0xff, trbi = (mi >> 8) & 0xff;
+        const unsigned int pmask = s.partner[trbi];
+        if (s.R2 > 0.f) for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
+          float dx[3], r2 = 0.f;
 #pragma unroll
-        for (int k = 0; k < D; k++) {
-          dx[k] = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
-          r2 += dx[k] * dx[k];
-        }
-        if (!(r2 < s.R2)) return;
-        if (st.mol[j] == moli) return;  // same molecule (and self)
-        const uint32_t mj = st.meta[j];
-        const int tj = mj & 0xff, trbj = (mj >> 8) & 0xff;
-        if (!((pmask >> trbj) & 1)) return;
-        const unsigned int pp = s.ppair[ti * MAXT + tj];
-        const int nl = pp & 31, l0 = pp >> 5;
-        if (!nl) return;
-        float fr = 0.f;
-        double dexact = -1.0;
-        for (int l = l0; l < l0 + nl; l++) {
-          const PairLaw& L = sh.laws[l];
-          if (r2 > L.rc2_hi) continue;
-          if (r2 >= L.rc2_lo) {
-            if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
-            if (dexact > L.rc) continue;
+          for (int k = 0; k < D; k++) {
+            dx[k] = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
+            r2 += dx[k] * dx[k];
           }
-          if (L.law == RDSIM_LAW_PIECEWISE_LINEAR) {
-            if (r2 < L.in2_lo) continue;
-            if (r2 <= L.in2_hi) {
+          if (!(r2 < s.R2)) return;
+          if (st.mol[j] == moli) return;  // same molecule (and self)
+          const uint32_t mj = st.meta[j];
+          const int tj = mj & 0xff, trbj = (mj >> 8) & 0xff;
+          if (!((pmask >> trbj) & 1)) return;
+          const unsigned int pp = s.ppair[ti * MAXT + tj];
+          const int nl = pp & 31, l0 = pp >> 5;
+          if (!nl) return;
+          float fr = 0.f;
+          double dexact = -1.0;
+          for (int l = l0; l < l0 + nl; l++) {
+            const PairLaw& L = sh.laws[l];
+            if (r2 > L.rc2_hi) continue;
+            if (r2 >= L.rc2_lo) {
               if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
-              if (dexact < L.rin) continue;
+              if (dexact > L.rc) continue;
+            }
+            if (L.law == RDSIM_LAW_PIECEWISE_LINEAR) {
+              if (r2 < L.in2_lo) continue;
+              if (r2 <= L.in2_hi) {
+                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+                if (dexact < L.rin) continue;
+              }
+            }
+            fr += eval_pair(L, r2);
+          }
+#pragma unroll
+          for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
+        });
+      }
+#pragma unroll
+      for (int o = TPP >> 1; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < D; k++) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+      }
+      if (active && lane_g == 0) {
+        oidx[pl] = idx;
+#pragma unroll
+        for (int k = 0; k < D; k++) ofr[k * a.cap + pl] = acc[k];
+      }
+    }
+    __syncthreads();
+    for (int pl = tid; pl < nch; pl += BLOCK) {
+      const int idx = oidx[pl];
+      const int gi = st.gi ? st.gi[idx] : idx;
+      const uint32_t mi = st.meta[idx];
+      const int ti = mi & 0xff;
+      const int pid = a.pid[gi];
+      float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < D; k++) acc[k] = ofr[k * a.cap + pl];
+      // walls (pyrdsim.pyx:1979-1986)
+      for (int w = 0; w < s.nwalls; w++) {
+        const WallLaw& W = sh.walls[w];
+        if (W.type != ti) continue;
+        const uint32_t h = st.xh[W.dim][idx];
+        float f;
+        if (W.law == RDSIM_LAW_WALL) {
+          float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
+          float e = expf(-2.0f * fabsf(z));
+          f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
+        } else {
+          // reflecting coordinates are signed (an initial position may be < 0)
+          float y = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) * s.unit_hi[W.dim];
+          if (y > W.rc_hi) continue;
+          if (y >= W.rc_lo) {
+            double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
+            if (yd > W.rc) continue;
+          }
+          float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
+          f = W.c0 / y * (-1.2f * s9 + 3.0f * s3);
+        }
+#pragma unroll
+        for (int k = 0; k < D; k++)
+          if (k == W.dim) acc[k] += -f;
+      }
+      // bonded terms (pyrdsim.pyx:2037-2066), gathered per participant
+      const int tm = mi >> 24;
+      if (tm != 0xff) {
+        const TmplDev& T = a.tmpl[tm];
+        const int loc = (mi >> 16) & 0xff;
+        const int mbase = pid - loc;
+        float xo[3];
+        for (int e = a.atomterm[T.atom0 + loc]; e < a.atomterm[T.atom0 + loc + 1]; e++) {
+          const int code = a.atomterm[e];
+          const TermDev& tr = a.terms[code >> 2];
+          const int role = code & 3;
+          if (tr.kind == RDSIM_TERM_BOND) {
+            const int other = a.slot_of[mbase + (role == 0 ? tr.j : tr.i)];
+            float d2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              xo[k] = (float)(int)(a.xh[k][other] - a.xh[k][gi]) * s.unit_hi[k];
+              d2 += xo[k] * xo[k];
+            }
+            const float d = sqrtf(d2);
+            const float f = tr.k0 * (d - tr.p0) / d;
+#pragma unroll
+            for (int k = 0; k < D; k++) acc[k] += f * xo[k];
+          } else {
+            const int s1 = a.slot_of[mbase + tr.i], s2 = a.slot_of[mbase + tr.j],
+                      s3 = a.slot_of[mbase + tr.k];
+            float v1[3], v2[3], n1 = 0.f, n2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              v1[k] = (float)(int)(a.xh[k][s1] - a.xh[k][s2]) * s.unit_hi[k];
+              v2[k] = (float)(int)(a.xh[k][s3] - a.xh[k][s2]) * s.unit_hi[k];
+              n1 += v1[k] * v1[k];
+              n2 += v2[k] * v2[k];
+            }
+            const float d21 = sqrtf(n1), d23 = sqrtf(n2);
+            float c = 0.f, sn;
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              v1[k] /= d21;
+              v2[k] /= d23;
+              c += v1[k] * v2[k];
+            }
+            if (D == 2) {
+              sn = fabsf(v1[0] * v2[1] - v1[1] * v2[0]);
+            } else if (D == 3) {
+              float cx = v1[1] * v2[2] - v1[2] * v2[1];
+              float cy = v1[2] * v2[0] - v1[0] * v2[2];
+              float cz = v1[0] * v2[1] - v1[1] * v2[0];
+              sn = sqrtf(cx * cx + cy * cy + cz * cz);
+            } else {
+              sn = 0.f;
+            }
+            const float theta = atan2f(sn, c);
+            float prefac;
+            if (s.angle_is_pi > 0 && !(theta < tr.thr)) {
+              const float dt_ = theta - tr.p0, d2_ = dt_ * dt_;
+              prefac = -tr.k0 / (1.0f - d2_ / 6.0f + d2_ * d2_ / 120.0f);
+            } else {
+              prefac = tr.k0 * (theta - tr.p0) / sn;
+            }
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              const float f1 = prefac / d21 * (v2[k] - c * v1[k]);
+              const float f3 = prefac / d23 * (v1[k] - c * v2[k]);
+              acc[k] += role == 0 ? f1 : (role == 2 ? f3 : -(f1 + f3));
             }
           }
-          fr += eval_pair(L, r2);
         }
+      }
+      if (a.flags & F_STORE_DRIFT) {
 #pragma unroll
-        for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
-      });
-    }
-#pragma unroll
-    for (int o = TPP >> 1; o > 0; o >>= 1) {
-#pragma unroll
-      for (int k = 0; k < D; k++) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-    }
-    if (!active || lane_g != 0) continue;
-    const int ti = mi & 0xff;
-    const int pid = a.pid[gi];
-    // walls (pyrdsim.pyx:1979-1986)
-    for (int w = 0; w < s.nwalls; w++) {
-      const WallLaw& W = sh.walls[w];
-      if (W.type != ti) continue;
-      const uint32_t h = a.xh[W.dim][gi];
-      float f;
-      if (W.law == RDSIM_LAW_WALL) {
-        float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
-        float e = expf(-2.0f * fabsf(z));
-        f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
-      } else {
-        float y = (float)h * s.unit_hi[W.dim];
-        if (y > W.rc_hi) continue;
-        if (y >= W.rc_lo) {
-          double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
-          if (yd > W.rc) continue;
-        }
-        float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
-        f = W.c0 / y * (-1.2f * s9 + 3.0f * s3);
+        for (int k = 0; k < D; k++) a.drift[k][gi] = acc[k];
       }
 #pragma unroll
       for (int k = 0; k < D; k++)
-        if (k == W.dim) acc[k] += -f;
-    }
-    // bonded terms (pyrdsim.pyx:2037-2066), gathered per participant
-    const int tm = mi >> 24;
-    if (tm != 0xff) {
-      const TmplDev& T = a.tmpl[tm];
-      const int loc = (mi >> 16) & 0xff;
-      const int base = pid - loc;
-      float xo[3];
-      for (int e = a.atomterm[T.atom0 + loc]; e < a.atomterm[T.atom0 + loc + 1]; e++) {
-        const int code = a.atomterm[e];
-        const TermDev& tr = a.terms[code >> 2];
-        const int role = code & 3;
-        if (tr.kind == RDSIM_TERM_BOND) {
-          const int other = a.slot_of[base + (role == 0 ? tr.j : tr.i)];
-          float d2 = 0.f;
+        if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], a.step);
+      if (a.flags & F_CHECK_SKIN) {
+        // displacement since the last rebuild: keeps every pair within range in
+        // adjacent cells and within rs of each other at that rebuild
 #pragma unroll
-          for (int k = 0; k < D; k++) {
-            xo[k] = (float)(int)(a.xh[k][other] - a.xh[k][gi]) * s.unit_hi[k];
-            d2 += xo[k] * xo[k];
-          }
-          const float d = sqrtf(d2);
-          const float f = tr.k0 * (d - tr.p0) / d;
-#pragma unroll
-          for (int k = 0; k < D; k++) acc[k] += f * xo[k];
-        } else {
-          const int s1 = a.slot_of[base + tr.i], s2 = a.slot_of[base + tr.j],
-                    s3 = a.slot_of[base + tr.k];
-          float v1[3], v2[3], n1 = 0.f, n2 = 0.f;
-#pragma unroll
-          for (int k = 0; k < D; k++) {
-            v1[k] = (float)(int)(a.xh[k][s1] - a.xh[k][s2]) * s.unit_hi[k];
-            v2[k] = (float)(int)(a.xh[k][s3] - a.xh[k][s2]) * s.unit_hi[k];
-            n1 += v1[k] * v1[k];
-            n2 += v2[k] * v2[k];
-          }
-          const float d21 = sqrtf(n1), d23 = sqrtf(n2);
-          float c = 0.f, sn;
-#pragma unroll
-          for (int k = 0; k < D; k++) {
-            v1[k] /= d21;
-            v2[k] /= d23;
-            c += v1[k] * v2[k];
-          }
-          if (D == 2) {
-            sn = fabsf(v1[0] * v2[1] - v1[1] * v2[0]);
-          } else {
-            float cx = v1[1] * v2[2] - v1[2] * v2[1];
-            float cy = v1[2] * v2[0] - v1[0] * v2[2];
-            float cz = v1[0] * v2[1] - v1[1] * v2[0];
-            sn = sqrtf(cx * cx + cy * cy + cz * cz);
-          }
-          const float theta = atan2f(sn, c);
-          float prefac;
-          if (s.angle_is_pi > 0 && !(theta < tr.thr)) {
-            const float dt_ = theta - tr.p0, d2_ = dt_ * dt_;
-            prefac = -tr.k0 / (1.0f - d2_ / 6.0f + d2_ * d2_ / 120.0f);
-          } else {
-            prefac = tr.k0 * (theta - tr.p0) / sn;
-          }
-#pragma unroll
-          for (int k = 0; k < D; k++) {
-            const float f1 = prefac / d21 * (v2[k] - c * v1[k]);
-            const float f3 = prefac / d23 * (v1[k] - c * v2[k]);
-            acc[k] += role == 0 ? f1 : (role == 2 ? f3 : -(f1 + f3));
-          }
+        for (int k = 0; k < D; k++) {
+          float rel = fabsf((float)(int)(st.xh[k][idx] - a.xr[k][gi])) * s.unit_hi[k];
+          if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, a.step);
         }
       }
+      if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, a.em_step, a.flags);
     }
-    if (a.flags & F_STORE_DRIFT) {
-#pragma unroll
-      for (int k = 0; k < D; k++) a.drift[k][gi] = acc[k];
-    }
-#pragma unroll
-    for (int k = 0; k < D; k++)
-      if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], a.step);
-    if (a.flags & F_CHECK_SKIN) {
-      // displacement since the last rebuild: keeps every pair within range in
-      // adjacent cells and within rs of each other at that rebuild
-#pragma unroll
-      for (int k = 0; k < D; k++) {
-        float rel = fabsf((float)(int)(a.xh[k][gi] - a.xr[k][gi])) * s.unit_hi[k];
-        if (rel > s.delta)
-          record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, a.step);
-      }
-    }
-    if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, a.em_step, a.flags);
+    __syncthreads();
   }
 }
 
 // ---------------------------------------------------------------------------
-// Reaction kernel: propensities from the current types, draws, new types.
+// Reaction kernel.  Phase A: TPP threads per own particle count, for every
+// neighbour-dependent reaction, the listed partners of the right type within
+// r0 (16-bit counters, two reactions per word).  Phase B: one thread per own
+// particle forms the float64 propensities in file order, draws and writes the
+// new type (pyrdsim.pyx:2091-2222).
 template <int D, int TPP>
-__global__ void __launch_bounds__(BLOCK) k_react(Args a) {
-  const TmplDev* tmpl = a.tmpl;
+__global__ void __launch_bounds__(BLOCK, 4) k_react(Args a) {
   extern __shared__ uint32_t dyn[];
   __shared__ TileShared<D> sh;
   const Tile t = a.tiles[blockIdx.x];
   Staged<D> st = tile_setup<D>(sh, a, t, dyn);
   const SysDev& s = sh.sys;
+  const TmplDev* tmpl = a.tmpl;
+  int* oidx = reinterpret_cast<int*>(dyn + (D + 3) * a.cap);
+  uint32_t* ocnt = dyn + (D + 4) * a.cap;  // [MAXR/2][cap]
   const int tid = threadIdx.x;
   const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
   const int nhc = sh.nhc, nown = sh.nown;
-  for (int p0 = 0; p0 < nown; p0 += groups) {
-    const int p = p0 + g;
-    const bool active = p < nown;
-    int cnt[MAXR];
+  for (int base = 0; base < nown; base += a.cap) {
+    const int nch = min(a.cap, nown - base);
+    for (int p0 = 0; p0 < nch; p0 += groups) {
+      const int pl = p0 + g;
+      const bool active = pl < nch;
+      uint32_t cnt[MAXR / 2] = {0u, 0u, 0u, 0u};
+      int idx = 0;
+      if (active) {
+        const int p = base + pl;
+        const int q = last_le(sh.own, nhc, p);
+        idx = sh.beg[q] + (p - sh.own[q]);
+        const uint32_t mi = st.meta[idx];
+        const int ti = mi & 0xff;
+        if ((s.rx_nb_mask >> ti) & 1) {
+          const int gi = st.gi ? st.gi[idx] : idx;
+          uint32_t xi_h[3];
 #pragma unroll
-    for (int r = 0; r < MAXR; r++) cnt[r] = 0;
-    int idx = 0, gi = 0;
-    uint32_t mi = 0;
-    if (active) {
-      const int q = last_le(sh.own, nhc, p);
-      idx = sh.beg[q] + (p - sh.own[q]);
-      gi = st.gi ? st.gi[idx] : idx;
-      mi = st.meta[idx];
-      const int ti = mi & 0xff;
-      if ((s.rx_nb_mask >> ti) & 1) {
-        uint32_t xi_h[3];
+          for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
+          const int moli = st.mol[idx];
+          const int trbi = (mi >> 8) & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
+          const unsigned int pmask = s.partner[trbi];
+          const uint32_t bmask = tmi != 0xff ? tmpl[tmi].bondmask[loci] : 0u;
+          for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
+            if (j == idx) return;
+            float r2 = 0.f;
 #pragma unroll
-        for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
-        const int moli = st.mol[idx];
-        const int trbi = (mi >> 8) & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
-        const unsigned int pmask = s.partner[trbi];
-        const uint32_t bmask = tmi != 0xff ? tmpl[tmi].bondmask[loci] : 0u;
-        for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
-          if (j == idx) return;
-          float r2 = 0.f;
-#pragma unroll
-          for (int k = 0; k < D; k++) {
-            float dx = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
-            r2 += dx * dx;
-          }
-          if (!(r2 < s.Rrx2)) return;
-          const uint32_t mj = st.meta[j];
-          bool listed;
-          if (st.mol[j] == moli) listed = (bmask >> ((mj >> 16) & 31)) & 1;
-          else listed = (pmask >> ((mj >> 8) & 0xff)) & 1;
-          if (!listed) return;
-          const int tj = mj & 0xff;
-          double dexact = -1.0;
-#pragma unroll
-          for (int r = 0; r < MAXR; r++) {
-            if (r >= s.nrx) break;
-            const RxDev& R = sh.rx[r];
-            if (R.reactant != ti) continue;
-            bool match = (R.kind == RDSIM_RX_CATALYZED && tj == R.catalyst) ||
-                         (R.kind == RDSIM_RX_INHIBITED && (tj == R.inh || tj == R.inh2));
-            if (!match) continue;
-            bool inside;
-            if (r2 < R.r02_lo) inside = true;
-            else if (r2 > R.r02_hi) inside = false;
-            else {
-              if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
-              inside = dexact < R.r0;
+            for (int k = 0; k < D; k++) {
+              float dx = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
+              r2 += dx * dx;
             }
-            cnt[r] += inside ? 1 : 0;
-          }
-        });
+            if (!(r2 < s.Rrx2)) return;
+            const uint32_t mj = st.meta[j];
+            bool listed;
+            if (st.mol[j] == moli) listed = (bmask >> ((mj >> 16) & 31)) & 1;
+            else listed = (pmask >> ((mj >> 8) & 0xff)) & 1;
+            if (!listed) return;
+            const int tj = mj & 0xff;
+            double dexact = -1.0;
+#pragma unroll
+            for (int r = 0; r < MAXR; r++) {
+              if (r >= s.nrx) break;
+              const RxDev& R = sh.rx[r];
+              if (R.reactant != ti) continue;
+              bool match = (R.kind == RDSIM_RX_CATALYZED && tj == R.catalyst) ||
+                           (R.kind == RDSIM_RX_INHIBITED && (tj == R.inh || tj == R.inh2));
+              if (!match) continue;
+              bool inside;
+              if (r2 < R.r02_lo) inside = true;
+              else if (r2 > R.r02_hi) inside = false;
+              else {
+                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+                inside = dexact < R.r0;
+              }
+              if (inside) cnt[r >> 1] += 1u << (16 * (r & 1));
+            }
+          });
+        }
+      }
+#pragma unroll
+      for (int w = 0; w < MAXR / 2; w++)
+#pragma unroll
+        for (int o = TPP >> 1; o > 0; o >>= 1) cnt[w] += __shfl_xor_sync(0xffffffffu, cnt[w], o);
+      if (active && lane_g == 0) {
+        oidx[pl] = idx;
+#pragma unroll
+        for (int w = 0; w < MAXR / 2; w++) ocnt[w * a.cap + pl] = cnt[w];
       }
     }
-#pragma unroll
-    for (int r = 0; r < MAXR; r++)
-#pragma unroll
-      for (int o = TPP >> 1; o > 0; o >>= 1) cnt[r] += __shfl_xor_sync(0xffffffffu, cnt[r], o);
-    if (!active || lane_g != 0) continue;
-    const int ti = mi & 0xff;
-    int newt = ti;
-    double total = 0.0;
-    double rate[MAXR];
-#pragma unroll
-    for (int r = 0; r < MAXR; r++) {  // pyrdsim.pyx:2091-2206, file order
-      rate[r] = 0.0;
-      if (r >= s.nrx) continue;
-      const RxDev& R = sh.rx[r];
-      double v = 0.0;
-      if (R.reactant == ti) {
-        if (R.kind == RDSIM_RX_LINEAR) {
-          v = R.rate;
-          total = __dadd_rn(total, R.rate);
-        } else if (R.kind == RDSIM_RX_CATALYZED) {
-          for (int c = 0; c < cnt[r]; c++) {
-            v = __dadd_rn(v, R.rate);
+    __syncthreads();
+    for (int pl = tid; pl < nch; pl += BLOCK) {
+      const int idx = oidx[pl];
+      const int gi = st.gi ? st.gi[idx] : idx;
+      const uint32_t mi = st.meta[idx];
+      const int ti = mi & 0xff;
+      int newt = ti;
+      double total = 0.0;
+      if ((s.rx_any_mask >> ti) & 1) {
+        for (int r = 0; r < s.nrx; r++) {  // pyrdsim.pyx:2091-2206, file order
+          const RxDev& R = sh.rx[r];
+          if (R.reactant != ti) continue;
+          if (R.kind == RDSIM_RX_LINEAR) {
             total = __dadd_rn(total, R.rate);
+          } else {
+            const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
+            if (R.kind == RDSIM_RX_CATALYZED) {
+              for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
+            } else {
+              double v = R.rate;
+              for (int e = 0; e < c; e++) v = __dsub_rn(v, R.dec);
+              if (v < 0) v = 0.0;
+              total = __dadd_rn(total, v);
+            }
           }
+        }
+      }
+      if (a.flags & F_RATES_ONLY) {
+        a.rates_out[a.pid[gi]] = total;
+        continue;
+      }
+      if ((s.rx_any_mask >> ti) & 1) {  // pyrdsim.pyx:2211-2222
+        const int pid = a.pid[gi];
+        double u1;
+        U4 w;
+        if (a.flags & F_INJECT) {
+          u1 = a.u1[pid];
         } else {
-          v = R.rate;
-          for (int c = 0; c < cnt[r]; c++) v = __dsub_rn(v, R.dec);
-          if (v < 0) v = 0.0;
-          total = __dadd_rn(total, v);
+          w = noise_words(s.seed, a.step, pid, 1u);
+          u1 = uniform53(w.x, w.y);
         }
-      }
-      rate[r] = v;
-    }
-    if (a.flags & F_RATES_ONLY) {
-      a.rates_out[a.pid[gi]] = total;
-      continue;
-    }
-    if ((s.rx_any_mask >> ti) & 1) {  // pyrdsim.pyx:2211-2222
-      const int pid = a.pid[gi];
-      double u1, u2;
-      U4 w;
-      if (a.flags & F_INJECT) {
-        u1 = a.u1[pid];
-      } else {
-        w = noise_words(s.seed, a.step, pid, 1u);
-        u1 = uniform53(w.x, w.y);
-      }
-      if (__dmul_rn(s.dt, total) > u1) {
-        u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
-        double acc = 0.0;
-        bool done = false;
-#pragma unroll
-        for (int r = 0; r < MAXR; r++) {
-          if (r >= s.nrx || done) continue;
-          acc = __dadd_rn(acc, __ddiv_rn(rate[r], total));
-          if (acc >= u2) {
-            newt = sh.rx[r].product;
-            done = true;
+        if (__dmul_rn(s.dt, total) > u1) {
+          const double u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
+          double acc = 0.0;
+          for (int r = 0; r < s.nrx; r++) {
+            const RxDev& R = sh.rx[r];
+            double v = 0.0;  // reaction_rates[r, particle]
+            if (R.reactant == ti) {
+              if (R.kind == RDSIM_RX_LINEAR) {
+                v = R.rate;
+              } else {
+                const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
+                if (R.kind == RDSIM_RX_CATALYZED) {
+                  for (int e = 0; e < c; e++) v = __dadd_rn(v, R.rate);
+                } else {
+                  v = R.rate;
+                  for (int e = 0; e < c; e++) v = __dsub_rn(v, R.dec);
+                  if (v < 0) v = 0.0;
+                }
+              }
+            }
+            acc = __dadd_rn(acc, __ddiv_rn(v, total));
+            if (acc >= u2) {
+              newt = R.product;
+              break;
+            }
           }
         }
       }
+      a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
     }
-    a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
+    __syncthreads();
   }
 }
 
