@@ -1312,3 +1312,89 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Neighbour pairs without allocation.
+//
+// rdsim_get_pairs allocates its device scratch (a pair counter and a pair
+// buffer) with cudaMalloc and releases it with cudaFree on every call.  Some
+// callers cannot do that: code that runs while another thread captures a
+// CUDA graph on the device, loops that must not pay the device-wide
+// synchronisation of cudaFree, or processes whose device memory is fully
+// committed to a preallocated pool.  rdsim_get_pairs_static computes the same
+// sorted pair list into the caller's host buffer with its scratch in the
+// static device array below instead.
+//
+// The array is RDSIM_STATIC_PAIRS_MAX pairs (8 MiB) plus a counter; every GPU
+// that loads the library holds it until the process exits.  Its device
+// address is looked up once per device (cudaGetSymbolAddress, with that device
+// current) by the first call on that device; make that first call before any
+// stream capture.  All calls share the array: the counter is cleared at the
+// start of every call, and calls that overlap on the GPU (from several
+// threads or handles at once) race on it.
+namespace {
+
+constexpr long long kStaticPairsMax = RDSIM_STATIC_PAIRS_MAX;
+// [0]: pair counter; [1 + p]: pair p as two int32 (i, j)
+static __device__ __align__(256) unsigned long long g_pairs_scratch[1 + kStaticPairsMax];
+
+constexpr int kMaxDevices = 64;
+unsigned long long* g_pairs_scratch_ptr[kMaxDevices] = {};
+
+int static_scratch(int device, unsigned long long** out) {
+  if (device < 0 || device >= kMaxDevices) return fail(RDSIM_ERR_ARG, "device ordinal out of range");
+  if (!g_pairs_scratch_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_pairs_scratch);
+    if (e != cudaSuccess)
+      return fail(RDSIM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_pairs_scratch_ptr[device] = static_cast<unsigned long long*>(p);
+  }
+  *out = g_pairs_scratch_ptr[device];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int rdsim_get_pairs_static(rdsim_handle* h, int32_t sys, int32_t* pairs,
+                                      int64_t cap, int64_t* n_pairs) {
+  if (!h || sys < 0 || sys >= h->nsys || !n_pairs) return fail(RDSIM_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  unsigned long long* scratch = nullptr;
+  int rc = static_scratch(h->device, &scratch);
+  if (rc) return rc;
+  const HostSys& q = h->hs[sys];
+  const SysDev& sd = h->sys_h[sys];
+  CK(cudaMemsetAsync(scratch, 0, sizeof(unsigned long long), h->stream));
+  double maxu = 0;
+  for (int k = 0; k < h->D; k++) maxu = std::max(maxu, (double)sd.unit_hi[k]);
+  const float rs2_hi = (float)(q.rs * q.rs) + guard2(q.rs, maxu);
+  Args a = make_args(h);
+  const unsigned g = nblk(q.n);
+  int* buf = reinterpret_cast<int*>(scratch + 1);
+  unsigned long long* cnt = scratch;
+  const unsigned long long lim = (unsigned long long)kStaticPairsMax;
+  if (h->D == 2) k_pairs<2><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, h->tmpl_d, q.rs, rs2_hi, q.p0, q.n, q.pid0, buf, lim, cnt);
+  else if (h->D == 3) k_pairs<3><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, h->tmpl_d, q.rs, rs2_hi, q.p0, q.n, q.pid0, buf, lim, cnt);
+  else k_pairs<1><<<g, 256, 0, h->stream>>>(h->sys_d, sys, a, h->tmpl_d, q.rs, rs2_hi, q.p0, q.n, q.pid0, buf, lim, cnt);
+  CK(cudaGetLastError());
+  unsigned long long n = 0;
+  CK(cudaMemcpyAsync(&n, cnt, sizeof n, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  *n_pairs = (int64_t)n;
+  if ((long long)n > kStaticPairsMax)
+    return fail(RDSIM_ERR_CAPACITY,
+                "rdsim_get_pairs_static: " + std::to_string(n) + " pairs exceed its static scratch of " +
+                    std::to_string(kStaticPairsMax) + " pairs; use rdsim_get_pairs");
+  if ((int64_t)n > cap) return fail(RDSIM_ERR_CAPACITY, "pair buffer too small");
+  if (n == 0 || !pairs) return 0;
+  CK(cudaMemcpyAsync(pairs, buf, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  // sort in the caller's buffer: (i, j) pairs of int32 viewed as one key each
+  struct P {
+    int32_t i, j;
+  };
+  P* v = reinterpret_cast<P*>(pairs);
+  std::sort(v, v + n, [](const P& x, const P& y) { return x.i != y.i ? x.i < y.i : x.j < y.j; });
+  return 0;
+}

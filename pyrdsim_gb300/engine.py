@@ -22,7 +22,7 @@ EXPORTS = [
     "rdsim_get_drift", "rdsim_get_reaction_rates", "rdsim_get_pairs", "rdsim_get_cell_ids",
     "rdsim_get_step", "rdsim_set_step", "rdsim_set_trajectory", "rdsim_get_trajectory",
     "rdsim_get_error", "rdsim_get_stream", "rdsim_get_info", "rdsim_last_error",
-    "rdsim_set_profiling", "rdsim_get_profile",
+    "rdsim_set_profiling", "rdsim_get_profile", "rdsim_get_pairs_static",
 ]
 
 
@@ -54,6 +54,7 @@ def load_library(path=None):
     L.rdsim_get_drift.argtypes = [vp, dp]
     L.rdsim_get_reaction_rates.argtypes = [vp, dp]
     L.rdsim_get_pairs.argtypes = [vp, C.c_int32, ip, C.c_int64, C.POINTER(C.c_int64)]
+    L.rdsim_get_pairs_static.argtypes = [vp, C.c_int32, ip, C.c_int64, C.POINTER(C.c_int64)]
     L.rdsim_get_cell_ids.argtypes = [vp, C.c_int32, ip]
     L.rdsim_get_step.argtypes = [vp, C.POINTER(C.c_int64)]
     L.rdsim_set_step.argtypes = [vp, C.c_int64]
