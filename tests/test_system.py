@@ -1,0 +1,162 @@
+"""The drop-in ``system`` class: deck parsing (CPU) and ``simulate()`` (GPU)."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import CASE_NAMES, deck_dict, in_deck, load_fixture
+
+REF_EXAMPLES = "/root/reference/examples"
+
+
+def test_parses_golden_decks_like_the_oracle_inputs():
+    from pyrdsim_gb300 import system
+    for name in CASE_NAMES:
+        fx = load_fixture(name)
+        with in_deck(deck_dict(fx)):
+            s = system({"seed": 1})
+            m = s._model
+            assert m.N_dim in (2, 3)
+            assert m.rs > 0 and m.N_traj == m.N_out // m.stride
+            assert len(m.interactions) >= 1
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+def test_parses_every_reference_example_deck():
+    """Every deck shipped with the reference parses, with the reference's
+    defaults (rs = 2 max_rc unless given, cell_length_ratio 2)."""
+    import glob
+    from pyrdsim_gb300 import decks, model
+    n = 0
+    for p in glob.glob(os.path.join(REF_EXAMPLES, "**", "parameters*.txt"), recursive=True):
+        d = os.path.dirname(p)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            prm = {"parameters_filename": os.path.basename(p)}
+            if not os.path.exists("nonbonded_interactions.txt"):
+                continue
+            if not os.path.exists("bonded_interactions.txt"):
+                continue
+            m = model.Model(prm)
+            assert m.N_dim == 2
+            if "rs" not in decks.load_parameters_file(
+                    p, decks.PARAMETERS_DATATYPES, [], decks.PARAMETERS_FLOAT_ARRAYS)[0]:
+                assert m.rs == 2 * m.max_rc
+            n += 1
+        finally:
+            os.chdir(cwd)
+    assert n >= 4
+
+
+def test_parser_errors_follow_reference():
+    from pyrdsim_gb300 import decks
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "nb.txt")
+        with open(p, "w") as f:
+            f.write("type = lj\n[interaction]\npair = 0 0\n")
+        with pytest.raises(RuntimeError, match="Parameter outside of section"):
+            decks.load_parameters_file(p, decks.NBINT_DATATYPES, decks.NBINT_INT_ARRAYS, [],
+                                       decks.NBINT_SECTION_KEYWORD)
+        with open(p, "w") as f:
+            f.write("[interaction]\nbogus = 1\n")
+        with pytest.raises(RuntimeError, match="Unrecognized entry"):
+            decks.load_parameters_file(p, decks.NBINT_DATATYPES, decks.NBINT_INT_ARRAYS, [],
+                                       decks.NBINT_SECTION_KEYWORD)
+        with open(p, "w") as f:
+            f.write("[interaction]\nu0 = 1 = 2\n")
+        with pytest.raises(RuntimeError, match="not of the form"):
+            decks.load_parameters_file(p, decks.NBINT_DATATYPES, decks.NBINT_INT_ARRAYS, [],
+                                       decks.NBINT_SECTION_KEYWORD)
+        ic = os.path.join(d, "ic.txt")
+        with open(ic, "w") as f:
+            f.write("0 0 0 3 1.0 2.0\n")
+        with pytest.raises(RuntimeError, match="friction coefficients"):
+            decks.load_initial_conditions(ic, 2, 2)
+        with pytest.raises(RuntimeError, match="inconsistent"):
+            decks.load_initial_conditions(ic, 3, 4)
+
+
+def test_deck_writer_round_trip():
+    """write_decks produces files that parse back to the same model."""
+    import tempfile
+    from pyrdsim_gb300 import model, workloads
+    sd = workloads.active_wall_fluid(n=256, seed=3)
+    m = sd.model
+    with tempfile.TemporaryDirectory() as d:
+        from pyrdsim_gb300 import decks
+        full = dict(m.parameters, interactions=m.interactions, reactions=m.reactions)
+        decks.write_decks(d, full, sd.x, sd.types, sd.molecule_ids)
+        cwd = os.getcwd()
+        os.chdir(d)
+        try:
+            m2 = model.Model({"seed": 1})
+            x, mol, t, first = decks.load_initial_conditions(
+                "initial_conditions.txt", 2, m2.N_species)
+        finally:
+            os.chdir(cwd)
+    assert np.array_equal(x, sd.x) and np.array_equal(t, sd.types)
+    assert m2.rs == m.rs and m2.N_reactions == m.N_reactions
+    assert [i["type"] for i in m2.interactions] == [i["type"] for i in m.interactions]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["lj_periodic", "angle_pi", "lj3d"])
+def test_simulate_without_noise_matches_oracle(name):
+    """random_force=False makes the run deterministic: simulate() on the GPU
+    follows the float64 oracle to 1e-6 over the whole run and stride frames."""
+    from oracle.oracle import Oracle
+    from pyrdsim_gb300 import model, system
+    fx = load_fixture(name)
+    with in_deck(deck_dict(fx)):
+        s = system({"seed": 1})
+        res = s.simulate(verbose=False, random_force=False)
+        sd = model.SystemData(s._model, *_ic(s))
+    o = Oracle(sd)
+    steps = s._model.N_steps
+    frames = []
+    for k in range(steps // s._model.stride):
+        o.step(s._model.stride, noise=False)
+        frames.append(o.state()[0])
+    L = sd.model.L
+    per = sd.model.periodic > 0
+
+    def dist(a, b):
+        d = a - b
+        d[:, per] -= L[per] * np.round(d[:, per] / L[per])
+        return np.abs(d).max()
+    assert dist(res["x"], o.state()[0]) < 1e-6
+    for k, f in enumerate(frames):
+        assert dist(res["trajectory"][k], f) < 1e-6
+    assert res["trajectory"].shape[1:] == sd.x.shape
+    assert set(res) == {"x", "particle_types", "trajectory", "trajectory_types",
+                        "molecule_ids", "first_index_of_molecule"}
+
+
+def _ic(s):
+    from pyrdsim_gb300 import decks
+    m = s._model
+    x, mol, t, first = decks.load_initial_conditions(m.initial_conditions_filename, m.N_dim,
+                                                     m.N_species)
+    return x, t, mol, first
+
+
+@pytest.mark.gpu
+def test_simulate_saves_and_appends_trajectory():
+    """N_out < N_steps: frames are saved every N_out//stride frames and
+    append=True continues from the saved state (pyrdsim.pyx:2429-2444)."""
+    fx = load_fixture("two_species_wall_rx")
+    texts = deck_dict(fx)
+    texts["parameters"] = texts["parameters"].replace("N_out = 100000", "N_out = 20")
+    from pyrdsim_gb300 import system
+    with in_deck(texts) as d:
+        s = system({"seed": 4})
+        res = s.simulate(verbose=False)
+        assert s.N_steps_completed == 40 and res["trajectory"].shape[0] == 2
+        s2 = system({"seed": 5})
+        res2 = s2.simulate(verbose=False, append=True)
+        assert s2.N_steps_completed == 40
+        files = os.listdir(d)
+        assert any(f.startswith("trajectory.h5") for f in files)
+    assert np.isfinite(res2["x"]).all()
