@@ -136,7 +136,8 @@ typedef struct rdsim_handle rdsim_handle;
 typedef struct {
   int32_t device;                 /* CUDA device ordinal                      */
   double skin;                    /* cell skin in length units; <= 0: auto    */
-  int32_t threads_per_particle;   /* 1, 2, 4 or 8; 0: auto                    */
+  int32_t threads_per_particle;   /* ignored: the pair loops use one warp per
+                                     own particle (reported as 32)            */
   int32_t tile_target;            /* target particles per tile; 0: auto       */
   int32_t use_graphs;             /* capture rebuild periods in CUDA graphs   */
   int32_t reserved[7];

@@ -27,7 +27,7 @@ constexpr int MAXI = RDSIM_MAX_INTERACTIONS;
 constexpr int MAXR = RDSIM_MAX_REACTIONS;
 constexpr int MAXA = RDSIM_MAX_ATOMS;
 constexpr int MAXW = 8;          // wall interactions per system
-constexpr int MAXHC = 256;       // halo cells per tile
+constexpr int MAXHC = 128;       // halo cells per tile
 constexpr int BLOCK = 128;       // threads per CTA of the tile kernels
 
 // One nonbonded pair law in evaluation form (pyrdsim.pyx:1068-1130).
@@ -95,13 +95,32 @@ struct SysDev {
   float fp[MAXT], npf[MAXT];      // dt*D and sqrt(2 dt D) per type
   unsigned int partner[MAXT];     // bit j of [i]: types i, j are partners
   unsigned short ppair[MAXT * MAXT];  // first law << 5 | count, symmetric
+  unsigned char rxmatch[MAXT * MAXT]; // bit r of [ti * MAXT + tj]: neighbour
+                                      // reaction r has reactant ti and counts tj
 };
 
+// One tile of cells of one system (static between create and destroy).  The
+// table offsets of its system are copied in so that every table load of a
+// tile kernel can be issued in the same round trip as the system itself.
 struct Tile {
   int sys;
   int c[3];
   int w[3];
+  int nhc;                        // halo cells (prod of hdim)
+  int hdim[3];
+  int law0, nlaws, wall0, nwalls, rx0, nrx;
   int pad;
+};
+
+// Per-tile staging plan, rebuilt with the cell list: for halo cell q (x
+// fastest) its first particle in the sorted arrays and count, the exclusive
+// prefix of counts over the halo (= its offset in shared memory) and the
+// exclusive prefix of interior (own) counts.
+struct PlanCell {
+  int beg, cnt, gbeg, own;
+};
+struct PlanHead {
+  int total, nown, pad0, pad1;
 };
 
 struct ErrDev {
@@ -121,6 +140,9 @@ struct Args {
   const TermDev* terms;
   const int* atomterm;            // term index * 4 + role, per template atom
   const int* cell_start;
+  const PlanCell* plan;           // [tile][plan_stride]
+  const PlanHead* plan_head;      // [tile]
+  int plan_stride;
   const uint32_t* xh[3];
   const uint32_t* xl[3];
   const uint32_t* meta;

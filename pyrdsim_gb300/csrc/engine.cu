@@ -86,6 +86,9 @@ struct rdsim_handle {
   int* atomterm_d = nullptr;
   int ncells = 0, nscan = 0;
   int *cell_count = nullptr, *cell_start = nullptr, *bsum = nullptr;
+  PlanCell* plan = nullptr;
+  PlanHead* plan_head = nullptr;
+  int plan_stride = 1;
   int *cell_of = nullptr, *rank_of = nullptr, *tmp = nullptr, *sid = nullptr, *slot_of = nullptr;
   uint32_t* xh[2][3] = {};
   uint32_t* xl[2][3] = {};
@@ -184,6 +187,9 @@ Args make_args(rdsim_handle* h) {
   a.terms = h->terms_d;
   a.atomterm = h->atomterm_d;
   a.cell_start = h->cell_start;
+  a.plan = h->plan;
+  a.plan_head = h->plan_head;
+  a.plan_stride = h->plan_stride;
   for (int k = 0; k < 3; k++) {
     a.xh[k] = h->xh[h->cx][k];
     a.xl[k] = h->xl[h->cx][k];
@@ -205,53 +211,32 @@ Args make_args(rdsim_handle* h) {
   return a;
 }
 
-template <int D, int TPP>
+template <int D>
 void set_smem_attrs(size_t dyn) {
-  cudaFuncSetAttribute(k_force<D, TPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-  cudaFuncSetAttribute(k_react<D, TPP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-}
-
-template <int D>
-int set_attrs_d(int tpp, size_t dyn) {
-  switch (tpp) {
-    case 1: set_smem_attrs<D, 1>(dyn); break;
-    case 2: set_smem_attrs<D, 2>(dyn); break;
-    case 4: set_smem_attrs<D, 4>(dyn); break;
-    case 8: set_smem_attrs<D, 8>(dyn); break;
-    default: return fail(RDSIM_ERR_ARG, "threads_per_particle must be 1, 2, 4 or 8");
-  }
-  return 0;
-}
-
-template <int D, int TPP>
-void launch_tile(rdsim_handle* h, bool react, const Args& a) {
-  dim3 grid((unsigned)h->tiles_h.size());
-  if (react) k_react<D, TPP><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-  else k_force<D, TPP><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-}
-
-template <int D>
-void launch_tile_d(rdsim_handle* h, bool react, const Args& a) {
-  switch (h->tpp) {
-    case 1: launch_tile<D, 1>(h, react, a); break;
-    case 2: launch_tile<D, 2>(h, react, a); break;
-    case 4: launch_tile<D, 4>(h, react, a); break;
-    default: launch_tile<D, 8>(h, react, a); break;
-  }
+  cudaFuncSetAttribute(k_force<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  cudaFuncSetAttribute(k_react<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
 }
 
 void launch_tiles(rdsim_handle* h, bool react, const Args& a) {
   if (h->tiles_h.empty()) return;
-  if (h->D == 2) launch_tile_d<2>(h, react, a);
-  else if (h->D == 3) launch_tile_d<3>(h, react, a);
-  else launch_tile_d<1>(h, react, a);
+  dim3 grid((unsigned)h->tiles_h.size());
+  if (h->D == 2) {
+    if (react) k_react<2><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+    else k_force<2><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+  } else if (h->D == 3) {
+    if (react) k_react<3><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+    else k_force<3><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+  } else {
+    if (react) k_react<1><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+    else k_force<1><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
+  }
 }
 
 unsigned nblk(int n, int b = 256) { return (unsigned)((n + b - 1) / b); }
 
 int rebuild(rdsim_handle* h) {
   const int n = h->N;
-  ProfScope ps(h, P_REBUILD, 5);
+  ProfScope ps(h, P_REBUILD, 6);
   CK(cudaMemsetAsync(h->cell_count, 0, sizeof(int) * (size_t)h->ncells, h->stream));
   uint32_t* const* x = h->xh[h->cx];
   if (h->D == 2)
@@ -272,6 +257,12 @@ int rebuild(rdsim_handle* h) {
   if (h->D == 2) k_order<2><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
   else if (h->D == 3) k_order<3><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
   else k_order<1><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
+  if (!h->tiles_h.empty()) {
+    const unsigned nt = (unsigned)h->tiles_h.size();
+    if (h->D == 2) k_plan<2><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
+    else if (h->D == 3) k_plan<3><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
+    else k_plan<1><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
+  }
   h->cx = 1 - h->cx;
   h->cm = 1 - h->cm;
   h->co = 1 - h->co;
@@ -438,6 +429,7 @@ void free_all(rdsim_handle* h) {
   F(h->sys_d); F(h->tiles_d); F(h->laws_d); F(h->walls_d); F(h->rx_d); F(h->tmpl_d);
   F(h->terms_d); F(h->atomterm_d); F(h->cell_count); F(h->cell_start); F(h->bsum);
   F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
+  F(h->plan); F(h->plan_head);
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
@@ -473,11 +465,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   h->device = opt.device;
   h->D = systems[0].n_dim;
   h->nsys = n_systems;
-  h->tpp = opt.threads_per_particle > 0 ? opt.threads_per_particle : 4;
-  if (h->tpp != 1 && h->tpp != 2 && h->tpp != 4 && h->tpp != 8) {
-    delete h;
-    return fail(RDSIM_ERR_ARG, "threads_per_particle must be 1, 2, 4 or 8");
-  }
+  h->tpp = 32;  // the pair loops run one warp per particle
   int rc = 0;
   auto bail = [&](int code) {
     free_all(h);
@@ -501,7 +489,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   std::vector<int> sid_h;
   int total_cells = 0;
   double skin_report = 0, cell_report = 1e300, range_report = 0;
-  int target = opt.tile_target > 0 ? opt.tile_target : 96;
+  int target = opt.tile_target > 0 ? opt.tile_target : 56;
 
   for (int si = 0; si < n_systems; si++) {
     const rdsim_system& S = systems[si];
@@ -711,6 +699,11 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         Rrx2 = std::max(Rrx2, x.r02_hi);
         R = std::max(R, r.r0);
         sd.rx_nb_mask |= 1 << r.reactant;
+        for (int tj = 0; tj < MAXT; tj++) {
+          const bool m = (r.kind == RDSIM_RX_CATALYZED && tj == r.catalyst) ||
+                         (r.kind == RDSIM_RX_INHIBITED && (tj == r.inhibitor || tj == r.inhibitor2));
+          if (m) sd.rxmatch[r.reactant * MAXT + tj] |= (unsigned char)(1u << q);
+        }
       }
       sd.rx_any_mask |= 1 << r.reactant;
       rxs.push_back(x);
@@ -793,10 +786,24 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
           std::memset(&t, 0, sizeof t);
           t.sys = si;
           int tt[3] = {tx, ty, tz};
+          t.nhc = 1;
+          for (int k = 0; k < 3; k++) {
+            t.w[k] = 1;
+            t.hdim[k] = 1;
+          }
           for (int k = 0; k < D; k++) {
             t.c[k] = tt[k] * w[k];
             t.w[k] = std::min(w[k], sd.nc[k] - t.c[k]);
+            t.hdim[k] = t.w[k] + 2 * sd.halo[k];
+            t.nhc *= t.hdim[k];
           }
+          t.law0 = sd.law0;
+          t.nlaws = sd.nlaws;
+          t.wall0 = sd.wall0;
+          t.nwalls = sd.nwalls;
+          t.rx0 = sd.rx0;
+          t.nrx = sd.nrx;
+          h->plan_stride = std::max(h->plan_stride, t.nhc);
           h->tiles_h.push_back(t);
         }
     sd.ntiles = (int)h->tiles_h.size() - sd.ntile0;
@@ -929,11 +936,13 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       const Tile& t = h->tiles_h[sd.ntile0];
       int hc = 1;
       for (int k = 0; k < D; k++) hc *= t.w[k] + 2 * sd.halo[k];
-      worst = std::max(worst, 4.0 * hc * (double)sd.n / ncs);
+      worst = std::max(worst, 2.5 * hc * (double)sd.n / ncs);
     }
     int cap = (int)std::ceil(worst / 256.0) * 256;
-    h->cap = std::max(512, std::min(4096, cap));
-    h->dyn_smem = (size_t)h->cap * (D + 4 + std::max(D, MAXR / 2)) * 4;
+    h->cap = std::max(256, std::min(4096, cap));
+    // staged records (4 words), sorted index, mol (D == 3), own index, and
+    // per-own-particle force (D words) or packed reaction counters (4 words)
+    h->dyn_smem = (size_t)h->cap * (7 + std::max(D, MAXR / 2)) * 4;
   }
   // device memory
   int64_t& B = h->device_bytes;
@@ -948,6 +957,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->atomterm_d, atomterm.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_count, (size_t)h->ncells, &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_start, (size_t)h->ncells + 1, &B))) return bail(rc);
+  if ((rc = dalloc(&h->plan, h->tiles_h.size() * (size_t)h->plan_stride, &B))) return bail(rc);
+  if ((rc = dalloc(&h->plan_head, h->tiles_h.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->bsum, (size_t)h->nscan, &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_of, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->rank_of, N, &B))) return bail(rc);
@@ -995,10 +1006,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   for (int k = 0; k < D; k++)
     if (cudaMemsetAsync(h->drift[k], 0, sizeof(float) * N, h->stream) != cudaSuccess)
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
-  if (D == 2) rc = set_attrs_d<2>(h->tpp, h->dyn_smem);
-  else if (D == 3) rc = set_attrs_d<3>(h->tpp, h->dyn_smem);
-  else rc = set_attrs_d<1>(h->tpp, h->dyn_smem);
-  if (rc) return bail(rc);
+  if (D == 2) set_smem_attrs<2>(h->dyn_smem);
+  else if (D == 3) set_smem_attrs<3>(h->dyn_smem);
+  else set_smem_attrs<1>(h->dyn_smem);
   if ((rc = upload_state(h, x_all, t_all))) return bail(rc);
   if ((rc = initial_drift(h))) return bail(rc);
   *out = h;

@@ -22,6 +22,14 @@
 
 #include "device.cuh"
 
+// resident CTAs per SM each tile kernel is compiled for (register budget)
+#ifndef RD_FORCE_MIN_BLOCKS
+#define RD_FORCE_MIN_BLOCKS 8
+#endif
+#ifndef RD_REACT_MIN_BLOCKS
+#define RD_REACT_MIN_BLOCKS 8
+#endif
+
 namespace rd {
 
 __device__ inline void record_error(ErrDev* e, int code, long long particle, int dim,
@@ -56,38 +64,38 @@ __device__ double exact_dist(const SysDev& s, const Args& a, int gi, int gj) {
   return __dsqrt_rn(d2);
 }
 
-// f / r of one pair law at squared distance r2 (float32).
-__device__ inline float eval_pair(const PairLaw& L, float r2) {
+// f / r of one pair law at squared distance r2 (float32); inv_r2 = 1 / r2.
+__device__ inline float eval_pair(const PairLaw& L, float r2, float inv_r2) {
   switch (L.law) {
     case RDSIM_LAW_LJ: {  // f = -2 n u0 / r * s (s - 1), s = (r0/r)^n
-      float q = L.c1 / r2;  // (r0/r)^2
+      const float q = L.c1 * inv_r2;  // (r0/r)^2
       float s;
-      if ((L.n & 1) == 0) {
+      if (L.n == 6) {
+        s = q * q * q;
+      } else if ((L.n & 1) == 0) {
         s = 1.0f;
         for (int e = 0; e < (L.n >> 1); e++) s *= q;
       } else {
-        float b = sqrtf(q);
+        const float b = sqrtf(q);
         s = 1.0f;
         for (int e = 0; e < L.n; e++) s *= b;
       }
-      return L.c0 * s * (s - 1.0f) / r2;
+      return L.c0 * s * (s - 1.0f) * inv_r2;
     }
     case RDSIM_LAW_TANH: {  // f = u0 (1 - tanh^2 z) / (2a), z = (r - r0)/a
-      float r = sqrtf(r2);
-      float z = (r - L.c1) * L.c2;
-      float e = expf(-2.0f * fabsf(z));
-      float sech2 = 4.0f * e / ((1.0f + e) * (1.0f + e));
-      return L.c0 * sech2 / r;
+      const float ir = rsqrtf(r2);
+      const float z = (r2 * ir - L.c1) * L.c2;
+      const float e = expf(-2.0f * fabsf(z));
+      return L.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e)) * ir;
     }
     case RDSIM_LAW_YUKAWA: {  // f = -u0 (1 + r0/r) exp(-r/r0) / (r r0)
-      float r = sqrtf(r2);
-      return L.c0 * (1.0f + L.c1 / r) * expf(-r * L.c2) / r2;
+      const float ir = rsqrtf(r2);
+      return L.c0 * (1.0f + L.c1 * ir) * expf(-r2 * ir * L.c2) * inv_r2;
     }
     case RDSIM_LAW_HARMONIC:  // f = u0 r
       return L.c0;
-    case RDSIM_LAW_PIECEWISE_LINEAR: {  // f = u0/dr for r >= r0 - dr
-      return L.c0 / sqrtf(r2);
-    }
+    case RDSIM_LAW_PIECEWISE_LINEAR:  // f = u0/dr for r >= r0 - dr
+      return L.c0 * rsqrtf(r2);
   }
   return 0.0f;
 }
@@ -132,136 +140,130 @@ struct TileShared {
   PairLaw laws[MAXI];
   WallLaw walls[MAXW];
   RxDev rx[MAXR];
-  int beg[MAXHC];
-  int cnt[MAXHC];
-  int gbeg[MAXHC];
-  int own[MAXHC];
-  int warp_tmp[BLOCK / 32];
+  PlanCell pc[MAXHC];
   int hdim[3];
   int nhc, total, nown, use_smem;
 };
 
+// Staged halo particles: one 16-byte record each.  D <= 2: {x0, x1, meta,
+// mol}; D == 3: {x0, x1, x2, meta} with mol in a separate array.  sgi holds
+// the particle's index in the sorted global arrays.
 template <int D>
 struct Staged {
-  const uint32_t* xh[D];
-  const uint32_t* meta;
-  const int* mol;
-  const int* gi;  // null: index is already global
+  uint4* sp;
+  int* smol;
+  int* sgi;
 };
 
-// Copy the system tables and stage the tile's halo.  Returns the source
-// arrays (shared memory, or global memory when the halo does not fit).
+__device__ inline void copy_words(int* dst, const int* src, int n) {
+  for (int q = threadIdx.x; q < n; q += BLOCK) dst[q] = src[q];
+}
+
+// Load the system, its tables and the tile's plan (one round trip), then
+// gather the halo particles into shared memory (a second one).
 template <int D>
 __device__ Staged<D> tile_setup(TileShared<D>& sh, const Args& a, const Tile& t,
                                 uint32_t* dyn) {
   const int tid = threadIdx.x;
-  {
-    const int* src = reinterpret_cast<const int*>(&a.sys[t.sys]);
-    int* dst = reinterpret_cast<int*>(&sh.sys);
-    for (int q = tid; q < (int)(sizeof(SysDev) / 4); q += BLOCK) dst[q] = src[q];
-  }
-  __syncthreads();
-  const SysDev& s = sh.sys;
-  {
-    const int* src = reinterpret_cast<const int*>(a.laws + s.law0);
-    int* dst = reinterpret_cast<int*>(sh.laws);
-    int nw = s.nlaws * (int)(sizeof(PairLaw) / 4);
-    for (int q = tid; q < nw; q += BLOCK) dst[q] = src[q];
-    src = reinterpret_cast<const int*>(a.walls + s.wall0);
-    dst = reinterpret_cast<int*>(sh.walls);
-    nw = s.nwalls * (int)(sizeof(WallLaw) / 4);
-    for (int q = tid; q < nw; q += BLOCK) dst[q] = src[q];
-    src = reinterpret_cast<const int*>(a.rx + s.rx0);
-    dst = reinterpret_cast<int*>(sh.rx);
-    nw = s.nrx * (int)(sizeof(RxDev) / 4);
-    for (int q = tid; q < nw; q += BLOCK) dst[q] = src[q];
-  }
+  copy_words(reinterpret_cast<int*>(&sh.sys), reinterpret_cast<const int*>(&a.sys[t.sys]),
+             (int)(sizeof(SysDev) / 4));
+  copy_words(reinterpret_cast<int*>(sh.laws), reinterpret_cast<const int*>(a.laws + t.law0),
+             t.nlaws * (int)(sizeof(PairLaw) / 4));
+  copy_words(reinterpret_cast<int*>(sh.walls), reinterpret_cast<const int*>(a.walls + t.wall0),
+             t.nwalls * (int)(sizeof(WallLaw) / 4));
+  copy_words(reinterpret_cast<int*>(sh.rx), reinterpret_cast<const int*>(a.rx + t.rx0),
+             t.nrx * (int)(sizeof(RxDev) / 4));
+  copy_words(reinterpret_cast<int*>(sh.pc),
+             reinterpret_cast<const int*>(a.plan + (size_t)blockIdx.x * a.plan_stride),
+             t.nhc * 4);
   if (tid == 0) {
-    int n = 1;
-    for (int k = 0; k < D; k++) {
-      sh.hdim[k] = t.w[k] + 2 * s.halo[k];
-      n *= sh.hdim[k];
-    }
-    sh.nhc = n;
+    const PlanHead hd = a.plan_head[blockIdx.x];
+    sh.total = hd.total;
+    sh.nown = hd.nown;
+    sh.nhc = t.nhc;
+    for (int k = 0; k < 3; k++) sh.hdim[k] = t.hdim[k];
+    sh.use_smem = hd.total <= a.cap ? 1 : 0;
   }
   __syncthreads();
-  const int nhc = sh.nhc;
-  for (int q = tid; q < MAXHC; q += BLOCK) {
-    int c = 0, g = 0, interior = 0;
-    if (q < nhc) {
-      bool inb = true;
-      interior = 1;
-      int rem = q, mult = 1;
-      for (int k = 0; k < D; k++) {
-        int hc = rem % sh.hdim[k];
-        rem /= sh.hdim[k];
-        if (hc < s.halo[k] || hc >= s.halo[k] + t.w[k]) interior = 0;
-        int ck = t.c[k] - s.halo[k] + hc;
-        if ((s.periodic >> k) & 1) {
-          if (ck < 0) ck += s.nc[k];
-          if (ck >= s.nc[k]) ck -= s.nc[k];
-        } else if (ck < 0 || ck >= s.nc[k]) {
-          inb = false;
-        }
-        g += ck * mult;
-        mult *= s.nc[k];
-      }
-      if (inb) {
-        int b = a.cell_start[s.c0 + g];
-        c = a.cell_start[s.c0 + g + 1] - b;
-        sh.gbeg[q] = b;
-      } else {
-        sh.gbeg[q] = 0;
-      }
-    }
-    sh.cnt[q] = c;
-    sh.beg[q] = c;
-    sh.own[q] = interior ? c : 0;
-  }
-  __syncthreads();
-  int total, nown;
-  scan_pairs(sh.beg, sh.warp_tmp, &sh.total);
-  total = sh.total;
-  scan_pairs(sh.own, sh.warp_tmp, &sh.nown);
-  nown = sh.nown;
-  (void)nown;
-  const bool use_smem = total <= a.cap;
   Staged<D> st;
-  if (use_smem) {
-    uint32_t* sx = dyn;
-    uint32_t* smeta = dyn + D * a.cap;
-    int* smol = reinterpret_cast<int*>(dyn + (D + 1) * a.cap);
-    int* sgi = reinterpret_cast<int*>(dyn + (D + 2) * a.cap);
+  st.sp = reinterpret_cast<uint4*>(dyn);
+  st.sgi = reinterpret_cast<int*>(dyn + 4 * a.cap);
+  st.smol = reinterpret_cast<int*>(dyn + 5 * a.cap);
+  if (sh.use_smem) {
+    const int total = sh.total, nhc = sh.nhc;
     for (int e = tid; e < total; e += BLOCK) {
-      int q = last_le(sh.beg, nhc, e);
-      int src = sh.gbeg[q] + (e - sh.beg[q]);
-#pragma unroll
-      for (int k = 0; k < D; k++) sx[k * a.cap + e] = a.xh[k][src];
-      smeta[e] = a.meta[src];
-      smol[e] = a.mol[src];
-      sgi[e] = src;
+      int lo = 0, hi = nhc;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (sh.pc[mid].beg <= e) lo = mid;
+        else hi = mid;
+      }
+      const int src = sh.pc[lo].gbeg + (e - sh.pc[lo].beg);
+      uint4 v;
+      v.x = a.xh[0][src];
+      v.y = D > 1 ? a.xh[1][src] : 0u;
+      if (D == 3) {
+        v.z = a.xh[2][src];
+        v.w = a.meta[src];
+        st.smol[e] = a.mol[src];
+      } else {
+        v.z = a.meta[src];
+        v.w = (uint32_t)a.mol[src];
+      }
+      st.sp[e] = v;
+      st.sgi[e] = src;
     }
-#pragma unroll
-    for (int k = 0; k < D; k++) st.xh[k] = sx + k * a.cap;
-    st.meta = smeta;
-    st.mol = smol;
-    st.gi = sgi;
-  } else {
-    for (int q = tid; q < nhc; q += BLOCK) sh.beg[q] = sh.gbeg[q];
-#pragma unroll
-    for (int k = 0; k < D; k++) st.xh[k] = a.xh[k];
-    st.meta = a.meta;
-    st.mol = a.mol;
-    st.gi = nullptr;
   }
-  if (tid == 0) sh.use_smem = use_smem ? 1 : 0;
   __syncthreads();
   return st;
 }
 
-// Visit every candidate neighbour of the own particle in halo cell `q`:
-// the 3^D (or fewer) cells around it.  fn(j) is called with the source index.
-template <int D, int TPP, class Fn>
+// Candidate data by index: shared records, or the global arrays when the
+// halo did not fit.
+template <int D, bool SMEM>
+__device__ inline void cand(const Staged<D>& st, const Args& a, int j, uint32_t* x,
+                            uint32_t& meta, int& mol) {
+  if (SMEM) {
+    const uint4 v = st.sp[j];
+    x[0] = v.x;
+    if (D > 1) x[1] = v.y;
+    if (D == 3) {
+      x[2] = v.z;
+      meta = v.w;
+      mol = st.smol[j];
+    } else {
+      meta = v.z;
+      mol = (int)v.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; k++) x[k] = a.xh[k][j];
+    meta = a.meta[j];
+    mol = a.mol[j];
+  }
+}
+
+template <int D, bool SMEM>
+__device__ inline int cand_gi(const Staged<D>& st, int j) {
+  return SMEM ? st.sgi[j] : j;
+}
+
+// Source index of own particle p (exclusive prefix of interior counts).
+template <bool SMEM>
+__device__ inline int own_index(const PlanCell* pc, int nhc, int p, int* qout) {
+  int lo = 0, hi = nhc;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (pc[mid].own <= p) lo = mid;
+    else hi = mid;
+  }
+  *qout = lo;
+  return (SMEM ? pc[lo].beg : pc[lo].gbeg) + (p - pc[lo].own);
+}
+
+// Visit every candidate neighbour of an own particle in halo cell q: the
+// 3^D (or fewer) cells around it; fn(j) gets the source index.
+template <int D, int TPP, bool SMEM, class Fn>
 __device__ inline void for_candidates(const TileShared<D>& sh, int q, int lane_g, Fn&& fn) {
   const SysDev& s = sh.sys;
   int hc[3] = {0, 0, 0};
@@ -280,13 +282,13 @@ __device__ inline void for_candidates(const TileShared<D>& sh, int q, int lane_g
       int rowbase = 0;
       if (D == 2) rowbase = (hc[1] + dy) * sh.hdim[0];
       if (D == 3) rowbase = ((hc[2] + dz) * sh.hdim[1] + (hc[1] + dy)) * sh.hdim[0];
-      int qa = rowbase + hc[0] - h0, qb = rowbase + hc[0] + h0;
-      if (sh.use_smem) {
-        int b = sh.beg[qa], e = sh.beg[qb] + sh.cnt[qb];
+      const int qa = rowbase + hc[0] - h0, qb = rowbase + hc[0] + h0;
+      if (SMEM) {
+        const int b = sh.pc[qa].beg, e = sh.pc[qb].beg + sh.pc[qb].cnt;
         for (int j = b + lane_g; j < e; j += TPP) fn(j);
       } else {
         for (int qq = qa; qq <= qb; qq++) {
-          int b = sh.beg[qq], e = b + sh.cnt[qq];
+          const int b = sh.pc[qq].gbeg, e = b + sh.pc[qq].cnt;
           for (int j = b + lane_g; j < e; j += TPP) fn(j);
         }
       }
@@ -376,22 +378,100 @@ __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid
 }
 
 // ---------------------------------------------------------------------------
+// Bonded terms of one particle (pyrdsim.pyx:2037-2066), gathered: the
+// particle evaluates every bond and angle it takes part in, reading its
+// partners' positions through slot_of (caller index -> sorted slot).
+template <int D>
+__device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int pid, uint32_t mi,
+                                    float* acc) {
+  const int tm = mi >> 24;
+  if (tm == 0xff) return;
+  const TmplDev& T = a.tmpl[tm];
+  const int loc = (mi >> 16) & 0xff;
+  const int mbase = pid - loc;
+  float xo[3];
+  for (int e = a.atomterm[T.atom0 + loc]; e < a.atomterm[T.atom0 + loc + 1]; e++) {
+    const int code = a.atomterm[e];
+    const TermDev& tr = a.terms[code >> 2];
+    const int role = code & 3;
+    if (tr.kind == RDSIM_TERM_BOND) {
+      const int other = a.slot_of[mbase + (role == 0 ? tr.j : tr.i)];
+      float d2 = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        xo[k] = (float)(int)(a.xh[k][other] - a.xh[k][gi]) * s.unit_hi[k];
+        d2 += xo[k] * xo[k];
+      }
+      const float d = sqrtf(d2);
+      const float f = tr.k0 * (d - tr.p0) / d;
+#pragma unroll
+      for (int k = 0; k < D; k++) acc[k] += f * xo[k];
+    } else {
+      const int s1 = a.slot_of[mbase + tr.i], s2 = a.slot_of[mbase + tr.j],
+                s3 = a.slot_of[mbase + tr.k];
+      float v1[3], v2[3], n1 = 0.f, n2 = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        v1[k] = (float)(int)(a.xh[k][s1] - a.xh[k][s2]) * s.unit_hi[k];
+        v2[k] = (float)(int)(a.xh[k][s3] - a.xh[k][s2]) * s.unit_hi[k];
+        n1 += v1[k] * v1[k];
+        n2 += v2[k] * v2[k];
+      }
+      const float d21 = sqrtf(n1), d23 = sqrtf(n2);
+      float c = 0.f, sn;
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        v1[k] /= d21;
+        v2[k] /= d23;
+        c += v1[k] * v2[k];
+      }
+      if (D == 2) {
+        sn = fabsf(v1[0] * v2[1] - v1[1] * v2[0]);
+      } else if (D == 3) {
+        const float cx = v1[1] * v2[2] - v1[2] * v2[1];
+        const float cy = v1[2] * v2[0] - v1[0] * v2[2];
+        const float cz = v1[0] * v2[1] - v1[1] * v2[0];
+        sn = sqrtf(cx * cx + cy * cy + cz * cz);
+      } else {
+        sn = 0.f;
+      }
+      // theta from atan2(|u1 x u2|, u1.u2): well conditioned near 0 and pi,
+      // where acos(h) loses half its digits in float32
+      const float theta = atan2f(sn, c);
+      float prefac;
+      if (s.angle_is_pi > 0 && !(theta < tr.thr)) {
+        const float dt_ = theta - tr.p0, d2_ = dt_ * dt_;
+        prefac = -tr.k0 / (1.0f - d2_ / 6.0f + d2_ * d2_ / 120.0f);
+      } else {
+        prefac = tr.k0 * (theta - tr.p0) / sn;
+      }
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        const float f1 = prefac / d21 * (v2[k] - c * v1[k]);
+        const float f3 = prefac / d23 * (v1[k] - c * v2[k]);
+        acc[k] += role == 0 ? f1 : (role == 2 ? f3 : -(f1 + f3));
+      }
+    }
+  }
+}
+
 // Drift kernel.  Phase A: TPP threads per own particle run the pair loop and
 // combine with shuffles into shared memory.  Phase B: one thread per own
 // particle adds walls and bonded terms, stores the drift and/or performs the
 // fused Euler-Maruyama update, so no lane idles in the per-particle tail.
-template <int D, int TPP>
-__global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
-  extern __shared__ uint32_t dyn[];
-  __shared__ TileShared<D> sh;
-  const Tile t = a.tiles[blockIdx.x];
-  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
+template <int D, int TPP, bool SMEM>
+__device__ void force_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a,
+                           uint32_t* dyn) {
   const SysDev& s = sh.sys;
-  int* oidx = reinterpret_cast<int*>(dyn + (D + 3) * a.cap);
-  float* ofr = reinterpret_cast<float*>(dyn + (D + 4) * a.cap);
+  int* oidx = reinterpret_cast<int*>(dyn + 6 * a.cap);
+  float* ofr = reinterpret_cast<float*>(dyn + 7 * a.cap);
   const int tid = threadIdx.x;
   const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
   const int nhc = sh.nhc, nown = sh.nown;
+  float unit[3];
+#pragma unroll
+  for (int k = 0; k < D; k++) unit[k] = s.unit_hi[k];
+  const float R2 = s.R2;
   for (int base = 0; base < nown; base += a.cap) {
     const int nch = min(a.cap, nown - base);
     for (int p0 = 0; p0 < nch; p0 += groups) {
@@ -400,49 +480,49 @@ __global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
       float acc[3] = {0.f, 0.f, 0.f};
       int idx = 0;
       if (active) {
-        const int p = base + pl;
-        const int q = last_le(sh.own, nhc, p);
-        idx = sh.beg[q] + (p - sh.own[q]);
-        const int gi = st.gi ? st.gi[idx] : idx;
-        uint32_t xi_h[3];
-#pragma unroll
-        for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
-        const uint32_t mi = st.meta[idx];
-        const int moli = st.mol[idx];
+        int q;
+        idx = own_index<SMEM>(sh.pc, nhc, base + pl, &q);
+        const int gi = cand_gi<D, SMEM>(st, idx);
+        uint32_t xi_h[3] = {0u, 0u, 0u}, mi;
+        int moli;
+        cand<D, SMEM>(st, a, idx, xi_h, mi, moli);
         const int ti = mi & 0xff, trbi = (mi >> 8) & 0xff;
         const unsigned int pmask = s.partner[trbi];
-        if (s.R2 > 0.f) for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
+        if (R2 > 0.f) for_candidates<D, TPP, SMEM>(sh, q, lane_g, [&](int j) {
+          uint32_t xj[3] = {0u, 0u, 0u}, mj;
+          int molj;
+          cand<D, SMEM>(st, a, j, xj, mj, molj);
           float dx[3], r2 = 0.f;
 #pragma unroll
           for (int k = 0; k < D; k++) {
-            dx[k] = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
+            dx[k] = (float)(int)(xj[k] - xi_h[k]) * unit[k];
             r2 += dx[k] * dx[k];
           }
-          if (!(r2 < s.R2)) return;
-          if (st.mol[j] == moli) return;  // same molecule (and self)
-          const uint32_t mj = st.meta[j];
+          if (!(r2 < R2)) return;
+          if (molj == moli) return;  // same molecule (and self)
           const int tj = mj & 0xff, trbj = (mj >> 8) & 0xff;
           if (!((pmask >> trbj) & 1)) return;
           const unsigned int pp = s.ppair[ti * MAXT + tj];
           const int nl = pp & 31, l0 = pp >> 5;
           if (!nl) return;
+          const float inv_r2 = __frcp_rn(r2);
           float fr = 0.f;
           double dexact = -1.0;
           for (int l = l0; l < l0 + nl; l++) {
             const PairLaw& L = sh.laws[l];
             if (r2 > L.rc2_hi) continue;
             if (r2 >= L.rc2_lo) {
-              if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+              if (dexact < 0) dexact = exact_dist<D>(s, a, gi, cand_gi<D, SMEM>(st, j));
               if (dexact > L.rc) continue;
             }
             if (L.law == RDSIM_LAW_PIECEWISE_LINEAR) {
               if (r2 < L.in2_lo) continue;
               if (r2 <= L.in2_hi) {
-                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, cand_gi<D, SMEM>(st, j));
                 if (dexact < L.rin) continue;
               }
             }
-            fr += eval_pair(L, r2);
+            fr += eval_pair(L, r2, inv_r2);
           }
 #pragma unroll
           for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
@@ -462,8 +542,10 @@ __global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
     __syncthreads();
     for (int pl = tid; pl < nch; pl += BLOCK) {
       const int idx = oidx[pl];
-      const int gi = st.gi ? st.gi[idx] : idx;
-      const uint32_t mi = st.meta[idx];
+      const int gi = cand_gi<D, SMEM>(st, idx);
+      uint32_t xo_h[3] = {0u, 0u, 0u}, mi;
+      int moli;
+      cand<D, SMEM>(st, a, idx, xo_h, mi, moli);
       const int ti = mi & 0xff;
       const int pid = a.pid[gi];
       float acc[3] = {0.f, 0.f, 0.f};
@@ -473,96 +555,32 @@ __global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
       for (int w = 0; w < s.nwalls; w++) {
         const WallLaw& W = sh.walls[w];
         if (W.type != ti) continue;
-        const uint32_t h = st.xh[W.dim][idx];
+        uint32_t h = xo_h[0];
+#pragma unroll
+        for (int k = 1; k < D; k++)
+          if (k == W.dim) h = xo_h[k];
         float f;
         if (W.law == RDSIM_LAW_WALL) {
-          float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
-          float e = expf(-2.0f * fabsf(z));
+          const float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
+          const float e = expf(-2.0f * fabsf(z));
           f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
         } else {
           // reflecting coordinates are signed (an initial position may be < 0)
-          float y = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) * s.unit_hi[W.dim];
+          const float y = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) *
+                          s.unit_hi[W.dim];
           if (y > W.rc_hi) continue;
           if (y >= W.rc_lo) {
-            double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
+            const double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
             if (yd > W.rc) continue;
           }
-          float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
+          const float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
           f = W.c0 / y * (-1.2f * s9 + 3.0f * s3);
         }
 #pragma unroll
         for (int k = 0; k < D; k++)
           if (k == W.dim) acc[k] += -f;
       }
-      // bonded terms (pyrdsim.pyx:2037-2066), gathered per participant
-      const int tm = mi >> 24;
-      if (tm != 0xff) {
-        const TmplDev& T = a.tmpl[tm];
-        const int loc = (mi >> 16) & 0xff;
-        const int mbase = pid - loc;
-        float xo[3];
-        for (int e = a.atomterm[T.atom0 + loc]; e < a.atomterm[T.atom0 + loc + 1]; e++) {
-          const int code = a.atomterm[e];
-          const TermDev& tr = a.terms[code >> 2];
-          const int role = code & 3;
-          if (tr.kind == RDSIM_TERM_BOND) {
-            const int other = a.slot_of[mbase + (role == 0 ? tr.j : tr.i)];
-            float d2 = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              xo[k] = (float)(int)(a.xh[k][other] - a.xh[k][gi]) * s.unit_hi[k];
-              d2 += xo[k] * xo[k];
-            }
-            const float d = sqrtf(d2);
-            const float f = tr.k0 * (d - tr.p0) / d;
-#pragma unroll
-            for (int k = 0; k < D; k++) acc[k] += f * xo[k];
-          } else {
-            const int s1 = a.slot_of[mbase + tr.i], s2 = a.slot_of[mbase + tr.j],
-                      s3 = a.slot_of[mbase + tr.k];
-            float v1[3], v2[3], n1 = 0.f, n2 = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              v1[k] = (float)(int)(a.xh[k][s1] - a.xh[k][s2]) * s.unit_hi[k];
-              v2[k] = (float)(int)(a.xh[k][s3] - a.xh[k][s2]) * s.unit_hi[k];
-              n1 += v1[k] * v1[k];
-              n2 += v2[k] * v2[k];
-            }
-            const float d21 = sqrtf(n1), d23 = sqrtf(n2);
-            float c = 0.f, sn;
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              v1[k] /= d21;
-              v2[k] /= d23;
-              c += v1[k] * v2[k];
-            }
-            if (D == 2) {
-              sn = fabsf(v1[0] * v2[1] - v1[1] * v2[0]);
-            } else if (D == 3) {
-              float cx = v1[1] * v2[2] - v1[2] * v2[1];
-              float cy = v1[2] * v2[0] - v1[0] * v2[2];
-              float cz = v1[0] * v2[1] - v1[1] * v2[0];
-              sn = sqrtf(cx * cx + cy * cy + cz * cz);
-            } else {
-              sn = 0.f;
-            }
-            const float theta = atan2f(sn, c);
-            float prefac;
-            if (s.angle_is_pi > 0 && !(theta < tr.thr)) {
-              const float dt_ = theta - tr.p0, d2_ = dt_ * dt_;
-              prefac = -tr.k0 / (1.0f - d2_ / 6.0f + d2_ * d2_ / 120.0f);
-            } else {
-              prefac = tr.k0 * (theta - tr.p0) / sn;
-            }
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              const float f1 = prefac / d21 * (v2[k] - c * v1[k]);
-              const float f3 = prefac / d23 * (v1[k] - c * v2[k]);
-              acc[k] += role == 0 ? f1 : (role == 2 ? f3 : -(f1 + f3));
-            }
-          }
-        }
-      }
+      bonded_terms<D>(s, a, gi, pid, mi, acc);
       if (a.flags & F_STORE_DRIFT) {
 #pragma unroll
         for (int k = 0; k < D; k++) a.drift[k][gi] = acc[k];
@@ -575,7 +593,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
         // adjacent cells and within rs of each other at that rebuild
 #pragma unroll
         for (int k = 0; k < D; k++) {
-          float rel = fabsf((float)(int)(st.xh[k][idx] - a.xr[k][gi])) * s.unit_hi[k];
+          const float rel = fabsf((float)(int)(xo_h[k] - a.xr[k][gi])) * unit[k];
           if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, a.step);
         }
       }
@@ -585,117 +603,146 @@ __global__ void __launch_bounds__(BLOCK, 4) k_force(Args a) {
   }
 }
 
+template <int D, int TPP = 4>
+__global__ void __launch_bounds__(BLOCK, RD_FORCE_MIN_BLOCKS) k_force(Args a) {
+  extern __shared__ __align__(16) uint32_t dyn[];
+  __shared__ TileShared<D> sh;
+  const Tile t = a.tiles[blockIdx.x];
+  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
+  if (sh.use_smem) force_tile<D, TPP, true>(sh, st, a, dyn);
+  else force_tile<D, TPP, false>(sh, st, a, dyn);
+}
+
 // ---------------------------------------------------------------------------
 // Reaction kernel.  Phase A: TPP threads per own particle count, for every
 // neighbour-dependent reaction, the listed partners of the right type within
 // r0 (16-bit counters, two reactions per word).  Phase B: one thread per own
 // particle forms the float64 propensities in file order, draws and writes the
 // new type (pyrdsim.pyx:2091-2222).
-template <int D, int TPP>
-__global__ void __launch_bounds__(BLOCK, 4) k_react(Args a) {
-  extern __shared__ uint32_t dyn[];
-  __shared__ TileShared<D> sh;
-  const Tile t = a.tiles[blockIdx.x];
-  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
+__device__ inline double rx_rate(const RxDev& R, int ti, int c) {
+  double v = 0.0;  // reaction_rates[r, particle]
+  if (R.reactant != ti) return v;
+  if (R.kind == RDSIM_RX_LINEAR) return R.rate;
+  if (R.kind == RDSIM_RX_CATALYZED) {
+    for (int e = 0; e < c; e++) v = __dadd_rn(v, R.rate);
+    return v;
+  }
+  v = R.rate;
+  for (int e = 0; e < c; e++) v = __dsub_rn(v, R.dec);
+  return v < 0 ? 0.0 : v;
+}
+
+template <int D, int TPP, bool SMEM>
+__device__ void react_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a,
+                           uint32_t* dyn) {
   const SysDev& s = sh.sys;
   const TmplDev* tmpl = a.tmpl;
-  int* oidx = reinterpret_cast<int*>(dyn + (D + 3) * a.cap);
-  uint32_t* ocnt = dyn + (D + 4) * a.cap;  // [MAXR/2][cap]
+  int* oidx = reinterpret_cast<int*>(dyn + 6 * a.cap);
+  uint32_t* ocnt = dyn + 7 * a.cap;  // [MAXR/2][cap]
   const int tid = threadIdx.x;
   const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
   const int nhc = sh.nhc, nown = sh.nown;
+  float unit[3];
+#pragma unroll
+  for (int k = 0; k < D; k++) unit[k] = s.unit_hi[k];
+  const float Rrx2 = s.Rrx2;
   for (int base = 0; base < nown; base += a.cap) {
     const int nch = min(a.cap, nown - base);
     for (int p0 = 0; p0 < nch; p0 += groups) {
       const int pl = p0 + g;
       const bool active = pl < nch;
-      uint32_t cnt[MAXR / 2] = {0u, 0u, 0u, 0u};
+      uint32_t c0 = 0u, c1 = 0u, c2 = 0u, c3 = 0u;  // two 16-bit counters each
       int idx = 0;
       if (active) {
-        const int p = base + pl;
-        const int q = last_le(sh.own, nhc, p);
-        idx = sh.beg[q] + (p - sh.own[q]);
-        const uint32_t mi = st.meta[idx];
+        int q;
+        idx = own_index<SMEM>(sh.pc, nhc, base + pl, &q);
+        uint32_t xi_h[3] = {0u, 0u, 0u}, mi;
+        int moli;
+        cand<D, SMEM>(st, a, idx, xi_h, mi, moli);
         const int ti = mi & 0xff;
         if ((s.rx_nb_mask >> ti) & 1) {
-          const int gi = st.gi ? st.gi[idx] : idx;
-          uint32_t xi_h[3];
-#pragma unroll
-          for (int k = 0; k < D; k++) xi_h[k] = st.xh[k][idx];
-          const int moli = st.mol[idx];
+          const int gi = cand_gi<D, SMEM>(st, idx);
           const int trbi = (mi >> 8) & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
           const unsigned int pmask = s.partner[trbi];
           const uint32_t bmask = tmi != 0xff ? tmpl[tmi].bondmask[loci] : 0u;
-          for_candidates<D, TPP>(sh, q, lane_g, [&](int j) {
+          for_candidates<D, TPP, SMEM>(sh, q, lane_g, [&](int j) {
             if (j == idx) return;
+            uint32_t xj[3] = {0u, 0u, 0u}, mj;
+            int molj;
+            cand<D, SMEM>(st, a, j, xj, mj, molj);
             float r2 = 0.f;
 #pragma unroll
             for (int k = 0; k < D; k++) {
-              float dx = (float)(int)(st.xh[k][j] - xi_h[k]) * s.unit_hi[k];
+              const float dx = (float)(int)(xj[k] - xi_h[k]) * unit[k];
               r2 += dx * dx;
             }
-            if (!(r2 < s.Rrx2)) return;
-            const uint32_t mj = st.meta[j];
+            if (!(r2 < Rrx2)) return;
             bool listed;
-            if (st.mol[j] == moli) listed = (bmask >> ((mj >> 16) & 31)) & 1;
+            if (molj == moli) listed = (bmask >> ((mj >> 16) & 31)) & 1;
             else listed = (pmask >> ((mj >> 8) & 0xff)) & 1;
             if (!listed) return;
-            const int tj = mj & 0xff;
+            const unsigned int rm = s.rxmatch[ti * MAXT + (mj & 0xff)];
             double dexact = -1.0;
-#pragma unroll
-            for (int r = 0; r < MAXR; r++) {
-              if (r >= s.nrx) break;
+            for (unsigned int mm = rm; mm; mm &= mm - 1u) {
+              const int r = __ffs(mm) - 1;
               const RxDev& R = sh.rx[r];
-              if (R.reactant != ti) continue;
-              bool match = (R.kind == RDSIM_RX_CATALYZED && tj == R.catalyst) ||
-                           (R.kind == RDSIM_RX_INHIBITED && (tj == R.inh || tj == R.inh2));
-              if (!match) continue;
               bool inside;
               if (r2 < R.r02_lo) inside = true;
               else if (r2 > R.r02_hi) inside = false;
               else {
-                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, st.gi ? st.gi[j] : j);
+                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, cand_gi<D, SMEM>(st, j));
                 inside = dexact < R.r0;
               }
-              if (inside) cnt[r >> 1] += 1u << (16 * (r & 1));
+              if (inside) {
+                const uint32_t inc = 1u << (16 * (r & 1));
+                switch (r >> 1) {
+                  case 0: c0 += inc; break;
+                  case 1: c1 += inc; break;
+                  case 2: c2 += inc; break;
+                  default: c3 += inc; break;
+                }
+              }
             }
           });
         }
       }
 #pragma unroll
-      for (int w = 0; w < MAXR / 2; w++)
-#pragma unroll
-        for (int o = TPP >> 1; o > 0; o >>= 1) cnt[w] += __shfl_xor_sync(0xffffffffu, cnt[w], o);
+      for (int o = TPP >> 1; o > 0; o >>= 1) {
+        c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        c3 += __shfl_xor_sync(0xffffffffu, c3, o);
+      }
       if (active && lane_g == 0) {
         oidx[pl] = idx;
-#pragma unroll
-        for (int w = 0; w < MAXR / 2; w++) ocnt[w * a.cap + pl] = cnt[w];
+        ocnt[0 * a.cap + pl] = c0;
+        ocnt[1 * a.cap + pl] = c1;
+        ocnt[2 * a.cap + pl] = c2;
+        ocnt[3 * a.cap + pl] = c3;
       }
     }
     __syncthreads();
     for (int pl = tid; pl < nch; pl += BLOCK) {
       const int idx = oidx[pl];
-      const int gi = st.gi ? st.gi[idx] : idx;
-      const uint32_t mi = st.meta[idx];
+      const int gi = cand_gi<D, SMEM>(st, idx);
+      uint32_t xo_h[3], mi;
+      int moli;
+      cand<D, SMEM>(st, a, idx, xo_h, mi, moli);
       const int ti = mi & 0xff;
       int newt = ti;
+      const bool any = (s.rx_any_mask >> ti) & 1;
       double total = 0.0;
-      if ((s.rx_any_mask >> ti) & 1) {
+      if (any) {
         for (int r = 0; r < s.nrx; r++) {  // pyrdsim.pyx:2091-2206, file order
           const RxDev& R = sh.rx[r];
           if (R.reactant != ti) continue;
+          const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
           if (R.kind == RDSIM_RX_LINEAR) {
             total = __dadd_rn(total, R.rate);
+          } else if (R.kind == RDSIM_RX_CATALYZED) {
+            for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
           } else {
-            const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
-            if (R.kind == RDSIM_RX_CATALYZED) {
-              for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
-            } else {
-              double v = R.rate;
-              for (int e = 0; e < c; e++) v = __dsub_rn(v, R.dec);
-              if (v < 0) v = 0.0;
-              total = __dadd_rn(total, v);
-            }
+            total = __dadd_rn(total, rx_rate(R, ti, c));
           }
         }
       }
@@ -703,7 +750,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_react(Args a) {
         a.rates_out[a.pid[gi]] = total;
         continue;
       }
-      if ((s.rx_any_mask >> ti) & 1) {  // pyrdsim.pyx:2211-2222
+      if (any) {  // pyrdsim.pyx:2211-2222
         const int pid = a.pid[gi];
         double u1;
         U4 w;
@@ -715,26 +762,12 @@ __global__ void __launch_bounds__(BLOCK, 4) k_react(Args a) {
         }
         if (__dmul_rn(s.dt, total) > u1) {
           const double u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
-          double acc = 0.0;
+          double accu = 0.0;
           for (int r = 0; r < s.nrx; r++) {
             const RxDev& R = sh.rx[r];
-            double v = 0.0;  // reaction_rates[r, particle]
-            if (R.reactant == ti) {
-              if (R.kind == RDSIM_RX_LINEAR) {
-                v = R.rate;
-              } else {
-                const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
-                if (R.kind == RDSIM_RX_CATALYZED) {
-                  for (int e = 0; e < c; e++) v = __dadd_rn(v, R.rate);
-                } else {
-                  v = R.rate;
-                  for (int e = 0; e < c; e++) v = __dsub_rn(v, R.dec);
-                  if (v < 0) v = 0.0;
-                }
-              }
-            }
-            acc = __dadd_rn(acc, __ddiv_rn(v, total));
-            if (acc >= u2) {
+            const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
+            accu = __dadd_rn(accu, __ddiv_rn(rx_rate(R, ti, c), total));
+            if (accu >= u2) {
               newt = R.product;
               break;
             }
@@ -744,6 +777,77 @@ __global__ void __launch_bounds__(BLOCK, 4) k_react(Args a) {
       a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
     }
     __syncthreads();
+  }
+}
+
+template <int D, int TPP = 4>
+__global__ void __launch_bounds__(BLOCK, RD_REACT_MIN_BLOCKS) k_react(Args a) {
+  extern __shared__ __align__(16) uint32_t dyn[];
+  __shared__ TileShared<D> sh;
+  const Tile t = a.tiles[blockIdx.x];
+  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
+  if (sh.use_smem) react_tile<D, TPP, true>(sh, st, a, dyn);
+  else react_tile<D, TPP, false>(sh, st, a, dyn);
+}
+
+// Per-tile staging plan, once per rebuild (see PlanCell).
+template <int D>
+__global__ void __launch_bounds__(BLOCK) k_plan(const SysDev* sysv, const Tile* tiles,
+                                                const int* cell_start, PlanCell* plan,
+                                                PlanHead* head, int stride) {
+  __shared__ int v[2 * BLOCK], o[2 * BLOCK], warp_tmp[BLOCK / 32], tot[2];
+  const Tile t = tiles[blockIdx.x];
+  const SysDev& s = sysv[t.sys];
+  const int tid = threadIdx.x;
+  int gb[2] = {0, 0};
+  for (int r = 0; r < 2; r++) {
+    const int q = tid + r * BLOCK;
+    int c = 0, interior = 0;
+    if (q < t.nhc) {
+      bool inb = true;
+      interior = 1;
+      int rem = q, g = 0, mult = 1;
+      for (int k = 0; k < D; k++) {
+        const int hc = rem % t.hdim[k];
+        rem /= t.hdim[k];
+        if (hc < s.halo[k] || hc >= s.halo[k] + t.w[k]) interior = 0;
+        int ck = t.c[k] - s.halo[k] + hc;
+        if ((s.periodic >> k) & 1) {
+          if (ck < 0) ck += s.nc[k];
+          if (ck >= s.nc[k]) ck -= s.nc[k];
+        } else if (ck < 0 || ck >= s.nc[k]) {
+          inb = false;
+        }
+        g += ck * mult;
+        mult *= s.nc[k];
+      }
+      if (inb) {
+        gb[r] = cell_start[s.c0 + g];
+        c = cell_start[s.c0 + g + 1] - gb[r];
+      }
+    }
+    v[q] = c;
+    o[q] = interior ? c : 0;
+  }
+  __syncthreads();
+  scan_pairs(v, warp_tmp, &tot[0]);
+  scan_pairs(o, warp_tmp, &tot[1]);
+  for (int r = 0; r < 2; r++) {
+    const int q = tid + r * BLOCK;
+    if (q >= t.nhc) continue;
+    PlanCell pc;
+    pc.beg = v[q];
+    pc.cnt = (q + 1 < 2 * BLOCK ? v[q + 1] : tot[0]) - v[q];
+    pc.gbeg = gb[r];
+    pc.own = o[q];
+    plan[(size_t)blockIdx.x * stride + q] = pc;
+  }
+  if (tid == 0) {
+    PlanHead h;
+    h.total = tot[0];
+    h.nown = tot[1];
+    h.pad0 = h.pad1 = 0;
+    head[blockIdx.x] = h;
   }
 }
 
