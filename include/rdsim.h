@@ -139,7 +139,8 @@ typedef struct {
   int32_t threads_per_particle;   /* ignored: the pair loops use one warp per
                                      own particle (reported as 32)            */
   int32_t tile_target;            /* target particles per tile; 0: auto       */
-  int32_t use_graphs;             /* capture rebuild periods in CUDA graphs   */
+  int32_t use_graphs;             /* >= 0: replay whole rebuild periods as CUDA
+                                     graphs (Philox noise); < 0: plain launches */
   int32_t reserved[7];
 } rdsim_options;
 

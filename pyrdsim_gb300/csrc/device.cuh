@@ -161,6 +161,8 @@ struct Args {
   const double* u2;
   long long step;                 // step number of this kernel's work
   long long em_step;              // step number of the fused EM update
+  const long long* step_base;     // graph replays: step numbers are offsets
+                                  // from this device counter
   int ntiles;
   int cap;                        // staged-particle capacity (smem)
   int n_total;

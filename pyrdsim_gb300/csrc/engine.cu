@@ -113,6 +113,15 @@ struct rdsim_handle {
   int traj_stride = 0, traj_frames = 0;
   double* traj_x = nullptr;
   int* traj_t = nullptr;
+  // CUDA graphs of whole rebuild periods (Philox noise only)
+  bool graphs = true;
+  long long* step_dev = nullptr;       // device step counter read by replays
+  long long step_dev_value = -1;       // its value once queued work has run
+  struct GraphEntry {
+    cudaGraphExec_t exec;
+    int64_t launches[RDSIM_PROFILE_CLASSES];
+  };
+  std::map<int, GraphEntry> graph_cache;
   // kernel accounting
   int64_t nlaunch[RDSIM_PROFILE_CLASSES] = {};
   bool prof = false;
@@ -270,8 +279,10 @@ int rebuild(rdsim_handle* h) {
   return 0;
 }
 
-int force(rdsim_handle* h, long long step, int flags, const double* xi_next) {
+// `rel`: step numbers are offsets from the device counter (graph capture)
+int force(rdsim_handle* h, long long step, int flags, const double* xi_next, bool rel = false) {
   Args a = make_args(h);
+  a.step_base = rel ? h->step_dev : nullptr;
   a.step = step;
   a.em_step = step + 1;
   a.flags = flags | F_CHECK_SKIN;
@@ -285,8 +296,10 @@ int force(rdsim_handle* h, long long step, int flags, const double* xi_next) {
   return 0;
 }
 
-int react(rdsim_handle* h, long long step, int flags, const double* u1, const double* u2) {
+int react(rdsim_handle* h, long long step, int flags, const double* u1, const double* u2,
+          bool rel = false) {
   Args a = make_args(h);
+  a.step_base = rel ? h->step_dev : nullptr;
   a.step = step;
   a.flags = flags;
   a.u1 = u1;
@@ -422,6 +435,64 @@ int initial_drift(rdsim_handle* h) {
   return check_device_error(h);
 }
 
+// True if a trajectory frame falls on a step in [a, b].
+bool snapshot_in(rdsim_handle* h, long long a, long long b) {
+  if (h->traj_frames <= 0) return false;
+  const long long first = ((a + h->traj_stride - 1) / h->traj_stride) * h->traj_stride;
+  return first <= b;
+}
+
+// One rebuild period (steps s .. s+freq-1, each ending with the fused EM
+// update of the next step) as a CUDA graph.  Graphs are cached per buffer
+// parity state; kernel step numbers are offsets from a device counter that
+// the graph advances by freq at its end.
+int run_period_graph(rdsim_handle* h, long long s, int kf) {
+  const int key = h->cx | (h->cm << 1) | (h->co << 2) | ((kf & F_NO_NOISE) ? 8 : 0);
+  auto it = h->graph_cache.find(key);
+  const int cx0 = h->cx, cm0 = h->cm, co0 = h->co;
+  if (it == h->graph_cache.end()) {
+    int64_t before[RDSIM_PROFILE_CLASSES];
+    std::memcpy(before, h->nlaunch, sizeof before);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = rebuild(h);
+    for (int i = 0; i < h->freq && !rc; i++) {
+      if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true);
+      if (!rc) rc = force(h, i, F_EM | kf, nullptr, true);
+    }
+    if (!rc) k_set_counter<<<1, 1, 0, h->stream>>>(h->step_dev, h->freq, 1);
+    cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ec != cudaSuccess) return fail(RDSIM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    rdsim_handle::GraphEntry e;
+    ec = cudaGraphInstantiate(&e.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ec != cudaSuccess) return fail(RDSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ec));
+    for (int c = 0; c < RDSIM_PROFILE_CLASSES; c++) {
+      e.launches[c] = h->nlaunch[c] - before[c];  // counted when replayed
+      h->nlaunch[c] = before[c];
+    }
+    it = h->graph_cache.emplace(key, e).first;
+    h->cx = cx0;
+    h->cm = cm0;
+    h->co = co0;
+  }
+  if (h->step_dev_value != s) k_set_counter<<<1, 1, 0, h->stream>>>(h->step_dev, s, 0);
+  CK(cudaGetLastError());
+  CK(cudaGraphLaunch(it->second.exec, h->stream));
+  h->step_dev_value = s + h->freq;
+  for (int c = 0; c < RDSIM_PROFILE_CLASSES; c++) h->nlaunch[c] += it->second.launches[c];
+  const int flips = (1 + h->freq) & 1;  // rebuild + freq updates / reactions
+  h->cx ^= flips;
+  if (h->has_rx) h->cm ^= flips;
+  else h->cm ^= 1;
+  h->co ^= 1;
+  return 0;
+}
+
 void free_all(rdsim_handle* h) {
   auto F = [](void* p) {
     if (p) cudaFree(p);
@@ -442,6 +513,9 @@ void free_all(rdsim_handle* h) {
     cudaEventDestroy(p.b);
   }
   for (auto e : h->ev_pool) cudaEventDestroy(e);
+  for (auto& g : h->graph_cache) cudaGraphExecDestroy(g.second.exec);
+  h->graph_cache.clear();
+  F(h->step_dev);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -982,6 +1056,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->xbuf, (size_t)N * D, &B))) return bail(rc);
   if ((rc = dalloc(&h->tbuf, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->err, 1, &B))) return bail(rc);
+  if ((rc = dalloc(&h->step_dev, 1, &B))) return bail(rc);
+  h->graphs = opt.use_graphs >= 0;
   if ((rc = dalloc(&h->cl_d, (size_t)3 * h->nsys, &B))) return bail(rc);
   auto up = [&](void* d, const void* s, size_t bytes) -> int {
     if (bytes == 0) return 0;
@@ -1067,10 +1143,17 @@ int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi
     }
   }
   int rc;
-  for (int q = 0; q < n_steps; q++) {
+  // first step: the stand-alone update with the drift left by the last call
+  if ((rc = em(h, h->step + 1, kf, dxi))) return rc;
+  const bool graphable = h->graphs && !inj && !h->prof;
+  for (int q = 0; q < n_steps;) {
     const long long s = h->step + 1;
-    if (q == 0) {
-      if ((rc = em(h, s, kf, dxi))) return rc;
+    const int left = n_steps - q;
+    if (graphable && s % h->freq == 0 && left > h->freq && !snapshot_in(h, s, s + h->freq - 1)) {
+      if ((rc = run_period_graph(h, s, kf))) return rc;
+      h->step = s + h->freq - 1;
+      q += h->freq;
+      continue;
     }
     if (s % h->freq == 0) {
       if ((rc = rebuild(h))) return rc;
@@ -1088,6 +1171,7 @@ int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi
     const double* xn = (dxi && !last) ? dxi + (size_t)(q + 1) * N * D : nullptr;
     if ((rc = force(h, s, last ? F_STORE_DRIFT | kf : F_EM | kf, xn))) return rc;
     h->step = s;
+    q++;
   }
   return check_device_error(h);
 }

@@ -42,6 +42,18 @@ __device__ inline void record_error(ErrDev* e, int code, long long particle, int
   }
 }
 
+__device__ inline long long eff_step(const Args& a) {
+  return a.step_base ? *a.step_base + a.step : a.step;
+}
+__device__ inline long long eff_em_step(const Args& a) {
+  return a.step_base ? *a.step_base + a.em_step : a.em_step;
+}
+
+__global__ void k_set_counter(long long* c, long long v, int add) {
+  if (add) *c += v;
+  else *c = v;
+}
+
 __device__ inline double fixed_to_double(const SysDev& s, int k, uint32_t h, uint32_t l) {
   unsigned long long X = ((unsigned long long)h << 32) | l;
   if ((s.periodic >> k) & 1) return __dmul_rn(__ull2double_rn(X), s.unit_d[k]);
@@ -587,17 +599,17 @@ __device__ void force_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a
       }
 #pragma unroll
       for (int k = 0; k < D; k++)
-        if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], a.step);
+        if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], eff_step(a));
       if (a.flags & F_CHECK_SKIN) {
         // displacement since the last rebuild: keeps every pair within range in
         // adjacent cells and within rs of each other at that rebuild
 #pragma unroll
         for (int k = 0; k < D; k++) {
           const float rel = fabsf((float)(int)(xo_h[k] - a.xr[k][gi])) * unit[k];
-          if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, a.step);
+          if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, eff_step(a));
         }
       }
-      if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, a.em_step, a.flags);
+      if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags);
     }
     __syncthreads();
   }
@@ -757,7 +769,7 @@ __device__ void react_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a
         if (a.flags & F_INJECT) {
           u1 = a.u1[pid];
         } else {
-          w = noise_words(s.seed, a.step, pid, 1u);
+          w = noise_words(s.seed, eff_step(a), pid, 1u);
           u1 = uniform53(w.x, w.y);
         }
         if (__dmul_rn(s.dt, total) > u1) {
