@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--n", type=int, default=65536)
     p.add_argument("--segment", type=int, default=SEGMENT)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ensemble", action="store_true")
     return p.parse_args()
 
 
@@ -185,6 +186,42 @@ def force_error(eng, sd):
     return {"norm": norm, "per_particle_rms_floor": per}
 
 
+def ensemble_comparison(local, steps=100, n_systems=512):
+    """Batched ensemble (all systems in one handle, one launch per kernel per
+    step) vs the plain per-system form (one handle per system, stepped one
+    system at a time), both on the GPU with Philox noise."""
+    import torch
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    sds = workloads.ensemble(n_systems=n_systems)
+    total = sum(s.n_particles for s in sds)
+    batch = Engine(sds, device=local)
+    batch.step(steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch.step(steps)
+    torch.cuda.synchronize()
+    t_b = time.perf_counter() - t0
+    batch.close()
+    engines = [Engine([s], device=local) for s in sds]
+    for e in engines:
+        e.step(steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e in engines:
+        e.step(steps)
+    torch.cuda.synchronize()
+    t_p = time.perf_counter() - t0
+    for e in engines:
+        e.close()
+    b = total * steps / t_b
+    p = total * steps / t_p
+    return {"n_systems": n_systems, "n_particles": total, "steps": steps,
+            "batched": b, "plain_per_system": p, "speedup": b / p, "unit": UNIT,
+            "workload": "512 systems, N log-uniform [256, 16384], density U[0.2, 0.7], "
+                        "kT U[0.5, 2], LJ or Yukawa, half with two-state reactions"}
+
+
 def run_ours(args, rank, ws, local):
     import numpy as np
     import torch
@@ -283,6 +320,12 @@ def run_ours(args, rank, ws, local):
             out["force_err_vs_fp64"] = force_error(eng, sd)
         except Exception as exc:
             out["force_err_vs_fp64"] = {"unavailable": str(exc)[:200]}
+    if rank == 0 and ws == 1 and not args.no_ensemble:
+        eng.close()
+        try:
+            out["ensemble"] = ensemble_comparison(local)
+        except Exception as exc:
+            out["ensemble"] = {"unavailable": str(exc)[:200]}
     if rank == 0:
         print(json.dumps(out))
 

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -220,10 +221,24 @@ Args make_args(rdsim_handle* h) {
   return a;
 }
 
+// The dynamic shared-memory limit is an attribute of the kernel on one device,
+// shared by every handle of the process: it is only ever raised, so that a
+// later handle with a smaller staging capacity does not invalidate the
+// launches of an earlier one.
 template <int D>
-void set_smem_attrs(size_t dyn) {
-  cudaFuncSetAttribute(k_force<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-  cudaFuncSetAttribute(k_react<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+int set_smem_attrs(int dev, size_t dyn) {
+  static std::mutex mu;
+  static std::map<int, size_t> have;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = have[dev];
+  if (dyn <= cur) return 0;
+  if (cudaFuncSetAttribute(k_force<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess ||
+      cudaFuncSetAttribute(k_react<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(RDSIM_ERR_CUDA, "cudaFuncSetAttribute(max dynamic shared memory) failed");
+  }
+  cur = dyn;
+  return 0;
 }
 
 void launch_tiles(rdsim_handle* h, bool react, const Args& a) {
@@ -1082,9 +1097,10 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   for (int k = 0; k < D; k++)
     if (cudaMemsetAsync(h->drift[k], 0, sizeof(float) * N, h->stream) != cudaSuccess)
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
-  if (D == 2) set_smem_attrs<2>(h->dyn_smem);
-  else if (D == 3) set_smem_attrs<3>(h->dyn_smem);
-  else set_smem_attrs<1>(h->dyn_smem);
+  if (D == 2) rc = set_smem_attrs<2>(h->device, h->dyn_smem);
+  else if (D == 3) rc = set_smem_attrs<3>(h->device, h->dyn_smem);
+  else rc = set_smem_attrs<1>(h->device, h->dyn_smem);
+  if (rc) return bail(rc);
   if ((rc = upload_state(h, x_all, t_all))) return bail(rc);
   if ((rc = initial_drift(h))) return bail(rc);
   *out = h;

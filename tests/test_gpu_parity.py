@@ -179,3 +179,24 @@ def test_graph_replay_is_bit_identical(name):
         np.testing.assert_array_equal(tp, tg)
     np.testing.assert_array_equal(plain.drift(), graph.drift())
     assert plain.step_index == graph.step_index == 71
+
+
+def test_handles_with_different_staging_capacity():
+    """The kernels' shared-memory limit is per device and process: handles
+    created later with a smaller staging capacity leave earlier ones
+    runnable, and each handle steps exactly like a fresh one."""
+    from pyrdsim_gb300 import workloads
+    sds = workloads.ensemble(n_systems=6, n_min=256, n_max=4096)
+    engines = [_engine([s], use_graphs=False) for s in sds]
+    caps = [e.info()["max_tile_particles"] for e in engines]
+    assert len(set(caps)) > 1, caps
+    big = int(np.argmax(caps))
+    # the largest-capacity handle, created before smaller ones, still steps
+    for e in engines:
+        e.step(12)
+    x0, t0 = engines[big].state()
+    fresh = _engine([sds[big]], use_graphs=False)
+    fresh.step(12)
+    xf, tf = fresh.state()
+    np.testing.assert_array_equal(x0, xf)
+    np.testing.assert_array_equal(t0, tf)
