@@ -136,12 +136,15 @@ typedef struct rdsim_handle rdsim_handle;
 typedef struct {
   int32_t device;                 /* CUDA device ordinal                      */
   double skin;                    /* cell skin in length units; <= 0: auto    */
-  int32_t threads_per_particle;   /* ignored: the pair loops use one warp per
-                                     own particle (reported as 32)            */
-  int32_t tile_target;            /* target particles per tile; 0: auto       */
+  int32_t threads_per_particle;   /* lanes sharing one particle's list: 1, 2,
+                                     4 or 8; other values: 2                  */
+  int32_t tile_target;            /* unused (kept for layout)                 */
   int32_t use_graphs;             /* >= 0: replay whole rebuild periods as CUDA
                                      graphs (Philox noise); < 0: plain launches */
-  int32_t reserved[7];
+  int32_t list_width;             /* Verlet-list entries stored per particle;
+                                     0: auto.  Longer rows are regenerated from
+                                     the cells each step (same results)       */
+  int32_t reserved[6];
 } rdsim_options;
 
 /* rdsim_step flags */

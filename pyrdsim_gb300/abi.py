@@ -108,7 +108,8 @@ class System(C.Structure):
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("skin", C.c_double),
                 ("threads_per_particle", C.c_int32), ("tile_target", C.c_int32),
-                ("use_graphs", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("use_graphs", C.c_int32), ("list_width", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class Info(C.Structure):

@@ -90,6 +90,7 @@ struct SysDev {
   unsigned long long hrange[3];   // high-word range used for cell mapping
   float R2;                       // candidate radius^2 (forces + reactions)
   float Rrx2;                     // reaction radius^2 (guarded)
+  float Rl2;                      // Verlet-list radius^2: range + 2 sqrt(D) delta
   double dt;
   unsigned long long seed;
   float fp[MAXT], npf[MAXT];      // dt*D and sqrt(2 dt D) per type
@@ -121,6 +122,14 @@ struct PlanCell {
 };
 struct PlanHead {
   int total, nown, pad0, pad1;
+};
+
+// A run of consecutive particles (sorted order) of one system, handled by one
+// CTA of the list kernels; the system's table offsets are copied in.
+struct Chunk {
+  int sys, beg, cnt;
+  int law0, nlaws, wall0, nwalls, rx0, nrx;
+  int pad[3];
 };
 
 struct ErrDev {
@@ -163,6 +172,14 @@ struct Args {
   long long em_step;              // step number of the fused EM update
   const long long* step_base;     // graph replays: step numbers are offsets
                                   // from this device counter
+  const Chunk* chunks;            // list kernels: CTA -> particle run
+  const int* nbr;                 // Verlet list (ELL, see list.cuh)
+  const int* ncnt;                // entries per particle (may exceed W)
+  int* nbr_out;
+  int* ncnt_out;
+  int W, npad;                    // list width and particle stride
+  int single;                     // one system: chunks follow from blockIdx
+  Chunk chunk1;                   // ... with these table offsets
   int ntiles;
   int cap;                        // staged-particle capacity (smem)
   int n_total;

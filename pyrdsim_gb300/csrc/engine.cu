@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -19,6 +20,7 @@
 #include "../../include/rdsim.h"
 #include "device.cuh"
 #include "kernels.cuh"
+#include "list.cuh"
 
 using namespace rd;
 
@@ -90,6 +92,15 @@ struct rdsim_handle {
   PlanCell* plan = nullptr;
   PlanHead* plan_head = nullptr;
   int plan_stride = 1;
+  // Verlet-list kernels
+  bool list = true;
+  int ltpp = 2;                      // lanes per particle
+  int W = 0;                         // list width (entries per particle)
+  int npad = 0;                      // particle stride of the list
+  std::vector<Chunk> chunks_h;
+  Chunk* chunks_d = nullptr;
+  int* nbr = nullptr;
+  int* ncnt = nullptr;
   int *cell_of = nullptr, *rank_of = nullptr, *tmp = nullptr, *sid = nullptr, *slot_of = nullptr;
   uint32_t* xh[2][3] = {};
   uint32_t* xl[2][3] = {};
@@ -218,6 +229,15 @@ Args make_args(rdsim_handle* h) {
   a.ntiles = (int)h->tiles_h.size();
   a.cap = h->cap;
   a.n_total = h->N;
+  a.chunks = h->chunks_d;
+  a.nbr = h->nbr;
+  a.ncnt = h->ncnt;
+  a.nbr_out = h->nbr;
+  a.ncnt_out = h->ncnt;
+  a.W = h->W;
+  a.npad = h->npad;
+  a.single = h->nsys == 1 ? 1 : 0;
+  if (!h->chunks_h.empty()) a.chunk1 = h->chunks_h[0];
   return a;
 }
 
@@ -241,7 +261,37 @@ int set_smem_attrs(int dev, size_t dyn) {
   return 0;
 }
 
+template <int D, int TPP>
+void launch_list(rdsim_handle* h, bool react, const Args& a) {
+  const dim3 grid((unsigned)h->chunks_h.size());
+  if (react) k_react_l<D, TPP><<<grid, LBLOCK, 0, h->stream>>>(a);
+  else k_force_l<D, TPP><<<grid, LBLOCK, 0, h->stream>>>(a);
+}
+
+template <int D>
+void launch_list_d(rdsim_handle* h, bool react, const Args& a) {
+  if (h->ltpp == 1) launch_list<D, 1>(h, react, a);
+  else if (h->ltpp == 2) launch_list<D, 2>(h, react, a);
+  else if (h->ltpp == 8) launch_list<D, 8>(h, react, a);
+  else launch_list<D, 4>(h, react, a);
+}
+
+template <int D>
+void launch_nlist(rdsim_handle* h, const Args& a) {
+  const dim3 grid((unsigned)h->chunks_h.size());
+  if (h->ltpp == 1) k_nlist<D, 1><<<grid, LBLOCK, 0, h->stream>>>(a);
+  else if (h->ltpp == 2) k_nlist<D, 2><<<grid, LBLOCK, 0, h->stream>>>(a);
+  else if (h->ltpp == 8) k_nlist<D, 8><<<grid, LBLOCK, 0, h->stream>>>(a);
+  else k_nlist<D, 4><<<grid, LBLOCK, 0, h->stream>>>(a);
+}
+
 void launch_tiles(rdsim_handle* h, bool react, const Args& a) {
+  if (h->list) {
+    if (h->D == 2) launch_list_d<2>(h, react, a);
+    else if (h->D == 3) launch_list_d<3>(h, react, a);
+    else launch_list_d<1>(h, react, a);
+    return;
+  }
   if (h->tiles_h.empty()) return;
   dim3 grid((unsigned)h->tiles_h.size());
   if (h->D == 2) {
@@ -281,6 +331,17 @@ int rebuild(rdsim_handle* h) {
   if (h->D == 2) k_order<2><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
   else if (h->D == 3) k_order<3><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
   else k_order<1><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
+  if (h->list) {
+    h->cx = 1 - h->cx;
+    h->cm = 1 - h->cm;
+    h->co = 1 - h->co;
+    const Args b = make_args(h);
+    if (h->D == 2) launch_nlist<2>(h, b);
+    else if (h->D == 3) launch_nlist<3>(h, b);
+    else launch_nlist<1>(h, b);
+    CK(cudaGetLastError());
+    return 0;
+  }
   if (!h->tiles_h.empty()) {
     const unsigned nt = (unsigned)h->tiles_h.size();
     if (h->D == 2) k_plan<2><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
@@ -515,7 +576,7 @@ void free_all(rdsim_handle* h) {
   F(h->sys_d); F(h->tiles_d); F(h->laws_d); F(h->walls_d); F(h->rx_d); F(h->tmpl_d);
   F(h->terms_d); F(h->atomterm_d); F(h->cell_count); F(h->cell_start); F(h->bsum);
   F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
-  F(h->plan); F(h->plan_head);
+  F(h->plan); F(h->plan_head); F(h->chunks_d); F(h->nbr); F(h->ncnt);
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
@@ -579,6 +640,14 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   int total_cells = 0;
   double skin_report = 0, cell_report = 1e300, range_report = 0;
   int target = opt.tile_target > 0 ? opt.tile_target : 56;
+  {
+    const char* alg = std::getenv("RDSIM_TILES");
+    h->list = !(alg && alg[0] == '1');
+  }
+  if (opt.threads_per_particle == 1 || opt.threads_per_particle == 2 ||
+      opt.threads_per_particle == 4 || opt.threads_per_particle == 8)
+    h->ltpp = opt.threads_per_particle;
+  double list_expect = 0;  // expected list entries per particle (densest system)
 
   for (int si = 0; si < n_systems; si++) {
     const rdsim_system& S = systems[si];
@@ -819,6 +888,16 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     range_report = std::max(range_report, R);
     // with no pair work the displacement check is off
     sd.delta = R > 0 ? (float)delta : 1e30f;
+    // Verlet-list radius: a pair within range at some step of a rebuild period
+    // was within range + 2 sqrt(D) delta at its start (plus float margin)
+    if (R > 0) {
+      const double rr = std::sqrt((double)std::max(R2, Rrx2)) + 2.0 * std::sqrt((double)D) * delta;
+      const double rl = rr * (1.0 + 1e-6) + 8.0 * max_unit;
+      sd.Rl2 = (float)(rl * rl);
+      double vol = 1.0, ball = D == 1 ? 2.0 * rl : (D == 2 ? M_PI * rl * rl : 4.0 / 3.0 * M_PI * rl * rl * rl);
+      for (int k = 0; k < D; k++) vol *= S.L[k];
+      list_expect = std::max(list_expect, std::min((double)S.n_particles, S.n_particles / vol * ball));
+    }
     // cells
     int ncs = 1;
     for (int k = 0; k < D; k++) {
@@ -1033,6 +1112,37 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     // per-own-particle force (D words) or packed reaction counters (4 words)
     h->dyn_smem = (size_t)h->cap * (7 + std::max(D, MAXR / 2)) * 4;
   }
+  // list kernels: CTA chunks per system; list width from the expected
+  // population (rows beyond it are regenerated from the cells)
+  if (h->list) {
+    const int per = LBLOCK / h->ltpp;
+    for (int si = 0; si < (int)h->sys_h.size(); si++) {
+      const SysDev& sd = h->sys_h[si];
+      for (int b = 0; b < sd.n; b += per) {
+        Chunk c;
+        std::memset(&c, 0, sizeof c);
+        c.sys = si;
+        c.beg = sd.p0 + b;
+        c.cnt = std::min(per, sd.n - b);
+        c.law0 = sd.law0;
+        c.nlaws = sd.nlaws;
+        c.wall0 = sd.wall0;
+        c.nwalls = sd.nwalls;
+        c.rx0 = sd.rx0;
+        c.nrx = sd.nrx;
+        h->chunks_h.push_back(c);
+      }
+    }
+    int W = (int)std::ceil(2.0 * list_expect + 16.0);
+    W = std::max(16, std::min(W, 2048));
+    h->npad = (h->N + 31) / 32 * 32;
+    const double limit = (double)(1 << 30);  // entries (32-bit list indices)
+    while (W > 16 && (double)W * h->npad > limit) W /= 2;
+    if (opt.list_width > 0) W = std::min(opt.list_width, 2048);
+    h->W = (W + 7) / 8 * 8;
+    if ((double)h->W * h->npad > limit)
+      return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many particles for the list kernels"));
+  }
   // device memory
   int64_t& B = h->device_bytes;
   const int N = h->N;
@@ -1072,6 +1182,11 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->tbuf, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->err, 1, &B))) return bail(rc);
   if ((rc = dalloc(&h->step_dev, 1, &B))) return bail(rc);
+  if (h->list) {
+    if ((rc = dalloc(&h->chunks_d, h->chunks_h.size(), &B))) return bail(rc);
+    if ((rc = dalloc(&h->nbr, (size_t)h->W * h->npad, &B))) return bail(rc);
+    if ((rc = dalloc(&h->ncnt, N, &B))) return bail(rc);
+  }
   h->graphs = opt.use_graphs >= 0;
   if ((rc = dalloc(&h->cl_d, (size_t)3 * h->nsys, &B))) return bail(rc);
   auto up = [&](void* d, const void* s, size_t bytes) -> int {
@@ -1084,6 +1199,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     for (int k = 0; k < D; k++) cl[3 * s + k] = h->hs[s].cl_ref[k];
   if ((rc = up(h->sys_d, h->sys_h.data(), sizeof(SysDev) * h->sys_h.size()))) return bail(rc);
   if ((rc = up(h->tiles_d, h->tiles_h.data(), sizeof(Tile) * h->tiles_h.size()))) return bail(rc);
+  if (h->list && (rc = up(h->chunks_d, h->chunks_h.data(), sizeof(Chunk) * h->chunks_h.size())))
+    return bail(rc);
   if ((rc = up(h->laws_d, laws.data(), sizeof(PairLaw) * laws.size()))) return bail(rc);
   if ((rc = up(h->walls_d, walls.data(), sizeof(WallLaw) * walls.size()))) return bail(rc);
   if ((rc = up(h->rx_d, rxs.data(), sizeof(RxDev) * rxs.size()))) return bail(rc);
@@ -1411,9 +1528,9 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
   std::memset(info, 0, sizeof *info);
   info->n_particles = h->N;
   info->n_cells = h->ncells;
-  info->n_tiles = (int64_t)h->tiles_h.size();
-  info->threads_per_particle = h->tpp;
-  info->max_tile_particles = h->cap;
+  info->n_tiles = h->list ? (int64_t)h->chunks_h.size() : (int64_t)h->tiles_h.size();
+  info->threads_per_particle = h->list ? h->ltpp : h->tpp;
+  info->max_tile_particles = h->list ? h->W : h->cap;
   info->skin = h->skin;
   info->cell_size_min = h->cell_min;
   info->interaction_range = h->range;

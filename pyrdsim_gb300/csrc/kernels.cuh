@@ -54,6 +54,16 @@ __global__ void k_set_counter(long long* c, long long v, int add) {
   else *c = v;
 }
 
+// Cell coordinate along dimension k of high word h.  Reflecting dimensions
+// hold signed values (an initial position may lie below 0 until the first
+// boundary step); those count as cell 0.
+__device__ inline int cell_coord(const SysDev& s, int k, uint32_t h) {
+  unsigned long long v = h;
+  if (!((s.periodic >> k) & 1) && (int)h < 0) v = 0;
+  const int c = (int)((v * (unsigned long long)s.nc[k]) / s.hrange[k]);
+  return c >= s.nc[k] ? s.nc[k] - 1 : c;
+}
+
 __device__ inline double fixed_to_double(const SysDev& s, int k, uint32_t h, uint32_t l) {
   unsigned long long X = ((unsigned long long)h << 32) | l;
   if ((s.periodic >> k) & 1) return __dmul_rn(__ull2double_rn(X), s.unit_d[k]);
@@ -110,6 +120,35 @@ __device__ inline float eval_pair(const PairLaw& L, float r2, float inv_r2) {
       return L.c0 * rsqrtf(r2);
   }
   return 0.0f;
+}
+
+// f / r summed over the laws of one type pair (pp = first << 5 | count) at
+// squared distance r2; near a cutoff the float64 distance decides
+// (pyrdsim.pyx:1988-2030).  gi, gj: sorted indices of the pair.
+template <int D>
+__device__ inline float pair_force(const SysDev& s, const PairLaw* laws, const Args& a, int gi,
+                                   int gj, unsigned int pp, float r2) {
+  const int nl = pp & 31, l0 = pp >> 5;
+  const float inv_r2 = __frcp_rn(r2);
+  float fr = 0.f;
+  double dexact = -1.0;
+  for (int l = l0; l < l0 + nl; l++) {
+    const PairLaw& L = laws[l];
+    if (r2 > L.rc2_hi) continue;
+    if (r2 >= L.rc2_lo) {
+      if (dexact < 0) dexact = exact_dist<D>(s, a, gi, gj);
+      if (dexact > L.rc) continue;
+    }
+    if (L.law == RDSIM_LAW_PIECEWISE_LINEAR) {
+      if (r2 < L.in2_lo) continue;
+      if (r2 <= L.in2_hi) {
+        if (dexact < 0) dexact = exact_dist<D>(s, a, gi, gj);
+        if (dexact < L.rin) continue;
+      }
+    }
+    fr += eval_pair(L, r2, inv_r2);
+  }
+  return fr;
 }
 
 // ---------------------------------------------------------------------------
@@ -467,6 +506,63 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
   }
 }
 
+// Per-particle tail of the drift kernels, on one thread per particle: walls
+// (pyrdsim.pyx:1979-1986), bonded terms, drift store, finiteness and skin
+// checks, and the fused Euler-Maruyama update.  acc holds the pair drift.
+template <int D>
+__device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const Args& a, int gi,
+                                  const uint32_t* xo_h, uint32_t mi, float* acc) {
+  const int ti = mi & 0xff;
+  const int pid = a.pid[gi];
+  // walls (pyrdsim.pyx:1979-1986)
+  for (int w = 0; w < s.nwalls; w++) {
+    const WallLaw& W = walls[w];
+    if (W.type != ti) continue;
+    uint32_t h = xo_h[0];
+#pragma unroll
+    for (int k = 1; k < D; k++)
+      if (k == W.dim) h = xo_h[k];
+    float f;
+    if (W.law == RDSIM_LAW_WALL) {
+      const float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
+      const float e = expf(-2.0f * fabsf(z));
+      f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
+    } else {
+      // reflecting coordinates are signed (an initial position may be < 0)
+      const float y = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) *
+                      s.unit_hi[W.dim];
+      if (y > W.rc_hi) continue;
+      if (y >= W.rc_lo) {
+        const double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
+        if (yd > W.rc) continue;
+      }
+      const float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
+      f = W.c0 / y * (-1.2f * s9 + 3.0f * s3);
+    }
+#pragma unroll
+    for (int k = 0; k < D; k++)
+      if (k == W.dim) acc[k] += -f;
+  }
+  bonded_terms<D>(s, a, gi, pid, mi, acc);
+  if (a.flags & F_STORE_DRIFT) {
+#pragma unroll
+    for (int k = 0; k < D; k++) a.drift[k][gi] = acc[k];
+  }
+#pragma unroll
+  for (int k = 0; k < D; k++)
+    if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], eff_step(a));
+  if (a.flags & F_CHECK_SKIN) {
+    // displacement since the last rebuild: keeps every pair within range in
+    // adjacent cells and within rs of each other at that rebuild
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      const float rel = fabsf((float)(int)(xo_h[k] - a.xr[k][gi])) * s.unit_hi[k];
+      if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, eff_step(a));
+    }
+  }
+  if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags);
+}
+
 // Drift kernel.  Phase A: TPP threads per own particle run the pair loop and
 // combine with shuffles into shared memory.  Phase B: one thread per own
 // particle adds walls and bonded terms, stores the drift and/or performs the
@@ -515,27 +611,8 @@ __device__ void force_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a
           const int tj = mj & 0xff, trbj = (mj >> 8) & 0xff;
           if (!((pmask >> trbj) & 1)) return;
           const unsigned int pp = s.ppair[ti * MAXT + tj];
-          const int nl = pp & 31, l0 = pp >> 5;
-          if (!nl) return;
-          const float inv_r2 = __frcp_rn(r2);
-          float fr = 0.f;
-          double dexact = -1.0;
-          for (int l = l0; l < l0 + nl; l++) {
-            const PairLaw& L = sh.laws[l];
-            if (r2 > L.rc2_hi) continue;
-            if (r2 >= L.rc2_lo) {
-              if (dexact < 0) dexact = exact_dist<D>(s, a, gi, cand_gi<D, SMEM>(st, j));
-              if (dexact > L.rc) continue;
-            }
-            if (L.law == RDSIM_LAW_PIECEWISE_LINEAR) {
-              if (r2 < L.in2_lo) continue;
-              if (r2 <= L.in2_hi) {
-                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, cand_gi<D, SMEM>(st, j));
-                if (dexact < L.rin) continue;
-              }
-            }
-            fr += eval_pair(L, r2, inv_r2);
-          }
+          if (!(pp & 31)) return;
+          const float fr = pair_force<D>(s, sh.laws, a, gi, cand_gi<D, SMEM>(st, j), pp, r2);
 #pragma unroll
           for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
         });
@@ -558,58 +635,10 @@ __device__ void force_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a
       uint32_t xo_h[3] = {0u, 0u, 0u}, mi;
       int moli;
       cand<D, SMEM>(st, a, idx, xo_h, mi, moli);
-      const int ti = mi & 0xff;
-      const int pid = a.pid[gi];
       float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int k = 0; k < D; k++) acc[k] = ofr[k * a.cap + pl];
-      // walls (pyrdsim.pyx:1979-1986)
-      for (int w = 0; w < s.nwalls; w++) {
-        const WallLaw& W = sh.walls[w];
-        if (W.type != ti) continue;
-        uint32_t h = xo_h[0];
-#pragma unroll
-        for (int k = 1; k < D; k++)
-          if (k == W.dim) h = xo_h[k];
-        float f;
-        if (W.law == RDSIM_LAW_WALL) {
-          const float z = (float)((long long)h - W.hr0) * s.unit_hi[W.dim] * W.c2;
-          const float e = expf(-2.0f * fabsf(z));
-          f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
-        } else {
-          // reflecting coordinates are signed (an initial position may be < 0)
-          const float y = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) *
-                          s.unit_hi[W.dim];
-          if (y > W.rc_hi) continue;
-          if (y >= W.rc_lo) {
-            const double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
-            if (yd > W.rc) continue;
-          }
-          const float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
-          f = W.c0 / y * (-1.2f * s9 + 3.0f * s3);
-        }
-#pragma unroll
-        for (int k = 0; k < D; k++)
-          if (k == W.dim) acc[k] += -f;
-      }
-      bonded_terms<D>(s, a, gi, pid, mi, acc);
-      if (a.flags & F_STORE_DRIFT) {
-#pragma unroll
-        for (int k = 0; k < D; k++) a.drift[k][gi] = acc[k];
-      }
-#pragma unroll
-      for (int k = 0; k < D; k++)
-        if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], eff_step(a));
-      if (a.flags & F_CHECK_SKIN) {
-        // displacement since the last rebuild: keeps every pair within range in
-        // adjacent cells and within rs of each other at that rebuild
-#pragma unroll
-        for (int k = 0; k < D; k++) {
-          const float rel = fabsf((float)(int)(xo_h[k] - a.xr[k][gi])) * unit[k];
-          if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, eff_step(a));
-        }
-      }
-      if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags);
+      force_tail<D>(s, sh.walls, a, gi, xo_h, mi, acc);
     }
     __syncthreads();
   }
@@ -642,6 +671,61 @@ __device__ inline double rx_rate(const RxDev& R, int ti, int c) {
   v = R.rate;
   for (int e = 0; e < c; e++) v = __dsub_rn(v, R.dec);
   return v < 0 ? 0.0 : v;
+}
+
+// Per-particle tail of the reaction kernels, on one thread per particle:
+// float64 propensities in file order, the draw and the new type
+// (pyrdsim.pyx:2091-2222).  cw holds the neighbour counts of the
+// neighbour-dependent reactions, two 16-bit counters per word.
+__device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& a, int gi,
+                                  uint32_t mi, const uint32_t* cw) {
+  const int ti = mi & 0xff;
+  int newt = ti;
+  const bool any = (s.rx_any_mask >> ti) & 1;
+  double total = 0.0;
+  if (any) {
+    for (int r = 0; r < s.nrx; r++) {  // pyrdsim.pyx:2091-2206, file order
+      const RxDev& R = rx[r];
+      if (R.reactant != ti) continue;
+      const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
+      if (R.kind == RDSIM_RX_LINEAR) {
+        total = __dadd_rn(total, R.rate);
+      } else if (R.kind == RDSIM_RX_CATALYZED) {
+        for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
+      } else {
+        total = __dadd_rn(total, rx_rate(R, ti, c));
+      }
+    }
+  }
+  if (a.flags & F_RATES_ONLY) {
+    a.rates_out[a.pid[gi]] = total;
+    return;
+  }
+  if (any) {  // pyrdsim.pyx:2211-2222
+    const int pid = a.pid[gi];
+    double u1;
+    U4 w;
+    if (a.flags & F_INJECT) {
+      u1 = a.u1[pid];
+    } else {
+      w = noise_words(s.seed, eff_step(a), pid, 1u);
+      u1 = uniform53(w.x, w.y);
+    }
+    if (__dmul_rn(s.dt, total) > u1) {
+      const double u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
+      double accu = 0.0;
+      for (int r = 0; r < s.nrx; r++) {
+        const RxDev& R = rx[r];
+        const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
+        accu = __dadd_rn(accu, __ddiv_rn(rx_rate(R, ti, c), total));
+        if (accu >= u2) {
+          newt = R.product;
+          break;
+        }
+      }
+    }
+  }
+  a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
 }
 
 template <int D, int TPP, bool SMEM>
@@ -740,53 +824,9 @@ __device__ void react_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a
       uint32_t xo_h[3], mi;
       int moli;
       cand<D, SMEM>(st, a, idx, xo_h, mi, moli);
-      const int ti = mi & 0xff;
-      int newt = ti;
-      const bool any = (s.rx_any_mask >> ti) & 1;
-      double total = 0.0;
-      if (any) {
-        for (int r = 0; r < s.nrx; r++) {  // pyrdsim.pyx:2091-2206, file order
-          const RxDev& R = sh.rx[r];
-          if (R.reactant != ti) continue;
-          const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
-          if (R.kind == RDSIM_RX_LINEAR) {
-            total = __dadd_rn(total, R.rate);
-          } else if (R.kind == RDSIM_RX_CATALYZED) {
-            for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
-          } else {
-            total = __dadd_rn(total, rx_rate(R, ti, c));
-          }
-        }
-      }
-      if (a.flags & F_RATES_ONLY) {
-        a.rates_out[a.pid[gi]] = total;
-        continue;
-      }
-      if (any) {  // pyrdsim.pyx:2211-2222
-        const int pid = a.pid[gi];
-        double u1;
-        U4 w;
-        if (a.flags & F_INJECT) {
-          u1 = a.u1[pid];
-        } else {
-          w = noise_words(s.seed, eff_step(a), pid, 1u);
-          u1 = uniform53(w.x, w.y);
-        }
-        if (__dmul_rn(s.dt, total) > u1) {
-          const double u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
-          double accu = 0.0;
-          for (int r = 0; r < s.nrx; r++) {
-            const RxDev& R = sh.rx[r];
-            const int c = (ocnt[(r >> 1) * a.cap + pl] >> (16 * (r & 1))) & 0xffff;
-            accu = __dadd_rn(accu, __ddiv_rn(rx_rate(R, ti, c), total));
-            if (accu >= u2) {
-              newt = R.product;
-              break;
-            }
-          }
-        }
-      }
-      a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
+      const uint32_t cw[4] = {ocnt[0 * a.cap + pl], ocnt[1 * a.cap + pl], ocnt[2 * a.cap + pl],
+                              ocnt[3 * a.cap + pl]};
+      react_tail(s, sh.rx, a, gi, mi, cw);
     }
     __syncthreads();
   }
@@ -891,14 +931,7 @@ __global__ void k_bin(const SysDev* sysv, const int* sid, const uint32_t* x0, co
     int g = 0, mult = 1;
 #pragma unroll
     for (int k = 0; k < D; k++) {
-      unsigned long long h = xs[k][i];
-      // reflecting dimensions hold signed values (an initial position may lie
-      // below 0 until the first boundary step)
-      if (!((s.periodic >> k) & 1) && (int)xs[k][i] < 0) h = 0;
-      int c = (int)((h * (unsigned long long)s.nc[k]) / s.hrange[k]);
-      if (c >= s.nc[k]) c = s.nc[k] - 1;
-      if (c < 0) c = 0;
-      g += c * mult;
+      g += cell_coord(s, k, xs[k][i]) * mult;
       mult *= s.nc[k];
     }
     gcell = s.c0 + g;

@@ -87,7 +87,7 @@ class Engine:
     """
 
     def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, tile_target=0,
-                 use_graphs=True):
+                 use_graphs=True, list_width=0):
         self.lib = load_library()
         self.systems = list(systems)
         self.D = self.systems[0].model.N_dim
@@ -100,6 +100,7 @@ class Engine:
         opt.threads_per_particle = threads_per_particle
         opt.tile_target = tile_target
         opt.use_graphs = 0 if use_graphs else -1
+        opt.list_width = list_width
         h = C.c_void_p()
         _check(self.lib.rdsim_create(arr, len(self.systems), C.byref(opt), C.byref(h)))
         self.h = h

@@ -200,3 +200,34 @@ def test_handles_with_different_staging_capacity():
     xf, tf = fresh.state()
     np.testing.assert_array_equal(x0, xf)
     np.testing.assert_array_equal(t0, tf)
+
+
+@pytest.mark.parametrize("name", ["two_species_wall_rx", "patchy", "mixed_laws"])
+def test_list_overflow_rows_match(name):
+    """Rows longer than the stored list width are regenerated from the cells
+    in the same order on the same lanes: results are bit-identical."""
+    fx, sd = _case(name)
+    full = _engine([sd], use_graphs=False)
+    short = _engine([sd], use_graphs=False, list_width=8)
+    assert short.info()["max_tile_particles"] == 8
+    np.testing.assert_array_equal(full.drift(), short.drift())
+    np.testing.assert_array_equal(full.reaction_rates(), short.reaction_rates())
+    for n in (7, 13):
+        full.step(n)
+        short.step(n)
+        xf, tf = full.state()
+        xs, ts = short.state()
+        np.testing.assert_array_equal(xf, xs)
+        np.testing.assert_array_equal(tf, ts)
+
+
+@pytest.mark.parametrize("tpp", [1, 4, 8])
+def test_lanes_per_particle_variants(tpp):
+    """1, 4 and 8 lanes per particle agree with the oracle like the default (2)."""
+    fx, sd = _case("mixed_laws")
+    eng = _engine([sd], threads_per_particle=tpp)
+    assert eng.info()["threads_per_particle"] == tpp
+    orc = _oracle(sd)
+    norm, per = drift_errors(eng.drift(), orc.drift())
+    assert norm <= FORCE_RTOL and per <= FORCE_RTOL, (norm, per)
+    np.testing.assert_array_equal(eng.reaction_rates(), orc.reaction_rates(recompute=True))
