@@ -45,8 +45,8 @@ enum {
   RDSIM_ERR_UNSUPPORTED = 4,  /* deck outside what the engine implements     */
   RDSIM_ERR_OUT_OF_BOUNDS = 16, /* particle outside the box (pyrdsim.pyx:2287) */
   RDSIM_ERR_ANGLE_DOMAIN = 17,  /* cos(angle) < -1.0000001 (pyrdsim.pyx:1365) */
-  RDSIM_ERR_SKIN = 18,        /* a particle left its cell by more than half
-                                 the skin between two rebuilds              */
+  RDSIM_ERR_SKIN = 18,        /* a particle moved more than half the skin
+                                 (Euclidean; dim = -1) between two rebuilds */
   RDSIM_ERR_NONFINITE = 19,   /* non-finite or larger-than-box displacement  */
   RDSIM_ERR_CAPACITY = 20     /* a per-call buffer was too small             */
 };
@@ -138,13 +138,19 @@ typedef struct {
   double skin;                    /* cell skin in length units; <= 0: auto    */
   int32_t threads_per_particle;   /* lanes sharing one particle's list: 1, 2,
                                      4 or 8; other values: 2                  */
-  int32_t tile_target;            /* unused (kept for layout)                 */
+  int32_t unused0;                /* 0                                        */
   int32_t use_graphs;             /* >= 0: replay whole rebuild periods as CUDA
                                      graphs (Philox noise); < 0: plain launches */
   int32_t list_width;             /* Verlet-list entries stored per particle;
                                      0: auto.  Longer rows are regenerated from
                                      the cells each step (same results)       */
-  int32_t reserved[6];
+  int32_t reaction_prefilter;     /* the drift kernel bounds each particle's
+                                     next reaction draw; the reaction kernel
+                                     then visits only the particles whose draw
+                                     may succeed (same results).  0: when few
+                                     draws are expected to pass the bound;
+                                     > 0: whenever the rates allow; < 0: off  */
+  int32_t reserved[5];
 } rdsim_options;
 
 /* rdsim_step flags */
@@ -238,13 +244,15 @@ int rdsim_get_error(rdsim_handle* h, int32_t* code, int64_t* particle,
 /* CUDA stream (cudaStream_t) that all work of the handle runs on. */
 int rdsim_get_stream(rdsim_handle* h, void** stream);
 
-/* Engine geometry chosen at create time, for reports: cell size, number of
- * cells, tiles, threads per particle, skin. */
+/* Engine geometry chosen at create time, for reports: cells, CTAs per step
+ * kernel, lanes per particle, Verlet-list width, skin, cell size. */
 typedef struct {
-  int64_t n_particles, n_cells, n_tiles;
-  int32_t threads_per_particle, max_tile_particles;
+  int64_t n_particles, n_cells, n_blocks;
+  int32_t threads_per_particle, list_width;
   double skin, cell_size_min, interaction_range;
   int64_t device_bytes;
+  int32_t reaction_prefilter;     /* 1: on for this handle                    */
+  int32_t pad;
 } rdsim_info;
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 

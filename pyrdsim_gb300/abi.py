@@ -107,17 +107,18 @@ class System(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("skin", C.c_double),
-                ("threads_per_particle", C.c_int32), ("tile_target", C.c_int32),
+                ("threads_per_particle", C.c_int32), ("unused0", C.c_int32),
                 ("use_graphs", C.c_int32), ("list_width", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("reaction_prefilter", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Info(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_cells", C.c_int64),
-                ("n_tiles", C.c_int64), ("threads_per_particle", C.c_int32),
-                ("max_tile_particles", C.c_int32), ("skin", C.c_double),
+                ("n_blocks", C.c_int64), ("threads_per_particle", C.c_int32),
+                ("list_width", C.c_int32), ("skin", C.c_double),
                 ("cell_size_min", C.c_double), ("interaction_range", C.c_double),
-                ("device_bytes", C.c_int64)]
+                ("device_bytes", C.c_int64), ("reaction_prefilter", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 PROFILE_CLASSES = 5

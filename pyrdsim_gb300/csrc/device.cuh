@@ -27,8 +27,7 @@ constexpr int MAXI = RDSIM_MAX_INTERACTIONS;
 constexpr int MAXR = RDSIM_MAX_REACTIONS;
 constexpr int MAXA = RDSIM_MAX_ATOMS;
 constexpr int MAXW = 8;          // wall interactions per system
-constexpr int MAXHC = 128;       // halo cells per tile
-constexpr int BLOCK = 128;       // threads per CTA of the tile kernels
+constexpr int BLOCK = 128;       // threads per CTA of the step kernels
 
 // One nonbonded pair law in evaluation form (pyrdsim.pyx:1068-1130).
 struct PairLaw {
@@ -68,7 +67,6 @@ struct TmplDev {
 struct SysDev {
   int p0, n;                      // particle range in the sorted arrays
   int c0;                         // first global cell
-  int ntile0, ntiles;
   int nc[3];                      // cells per dimension
   int halo[3];                    // 1, or 0 where nc == 1 and periodic
   int ntypes;
@@ -85,43 +83,24 @@ struct SysDev {
   long long Si[3];                // reflecting: fixed value of L
   float unit_hi[3];               // length per high-word unit
   float inv_unit_hi[3];
-  float delta;                    // allowed displacement per dimension since
-                                  // the last rebuild (length units)
+  float delta;                    // allowed displacement since the last
+                                  // rebuild (Euclidean, length units)
   unsigned long long hrange[3];   // high-word range used for cell mapping
   float R2;                       // candidate radius^2 (forces + reactions)
   float Rrx2;                     // reaction radius^2 (guarded)
-  float Rl2;                      // Verlet-list radius^2: range + 2 sqrt(D) delta
+  float Rl2;                      // Verlet-list radius^2: range + 2 delta
   double dt;
   unsigned long long seed;
   float fp[MAXT], npf[MAXT];      // dt*D and sqrt(2 dt D) per type
   unsigned int partner[MAXT];     // bit j of [i]: types i, j are partners
   unsigned short ppair[MAXT * MAXT];  // first law << 5 | count, symmetric
+  float prc2[MAXT * MAXT];        // largest guarded rc^2 of the pair's laws
   unsigned char rxmatch[MAXT * MAXT]; // bit r of [ti * MAXT + tj]: neighbour
                                       // reaction r has reactant ti and counts tj
-};
-
-// One tile of cells of one system (static between create and destroy).  The
-// table offsets of its system are copied in so that every table load of a
-// tile kernel can be issued in the same round trip as the system itself.
-struct Tile {
-  int sys;
-  int c[3];
-  int w[3];
-  int nhc;                        // halo cells (prod of hdim)
-  int hdim[3];
-  int law0, nlaws, wall0, nwalls, rx0, nrx;
-  int pad;
-};
-
-// Per-tile staging plan, rebuilt with the cell list: for halo cell q (x
-// fastest) its first particle in the sorted arrays and count, the exclusive
-// prefix of counts over the halo (= its offset in shared memory) and the
-// exclusive prefix of interior (own) counts.
-struct PlanCell {
-  int beg, cnt, gbeg, own;
-};
-struct PlanHead {
-  int total, nown, pad0, pad1;
+  // Upper bound of a particle's total propensity for the reaction prefilter:
+  // rxA[t] + rxB[t] * (listed neighbours) >= the float64 total of a type-t
+  // particle (linear and inhibited rates in rxA, catalysed rates in rxB).
+  double rxA[MAXT], rxB[MAXT];
 };
 
 // A run of consecutive particles (sorted order) of one system, handled by one
@@ -138,10 +117,9 @@ struct ErrDev {
   double value;
 };
 
-// Kernel arguments shared by the tile kernels (passed by value).
+// Kernel arguments shared by the step kernels (passed by value).
 struct Args {
   const SysDev* sys;
-  const Tile* tiles;
   const PairLaw* laws;
   const WallLaw* walls;
   const RxDev* rx;
@@ -149,9 +127,6 @@ struct Args {
   const TermDev* terms;
   const int* atomterm;            // term index * 4 + role, per template atom
   const int* cell_start;
-  const PlanCell* plan;           // [tile][plan_stride]
-  const PlanHead* plan_head;      // [tile]
-  int plan_stride;
   const uint32_t* xh[3];
   const uint32_t* xl[3];
   const uint32_t* meta;
@@ -178,10 +153,13 @@ struct Args {
   int* nbr_out;
   int* ncnt_out;
   int W, npad;                    // list width and particle stride
+  int4* rx_list;                  // [2][npad]: particles whose reaction draw
+                                  // may succeed at a step of that parity, as
+                                  // {sorted index, meta, list entries, pid}
+  int* rx_count;                  // [2]
+  const int* sid;                 // system of each particle
   int single;                     // one system: chunks follow from blockIdx
   Chunk chunk1;                   // ... with these table offsets
-  int ntiles;
-  int cap;                        // staged-particle capacity (smem)
   int n_total;
   int flags;
 };
@@ -192,7 +170,10 @@ enum : int {
   F_NO_NOISE = 4,                 // random_force = False
   F_INJECT = 8,                   // xi / u1 / u2 come from buffers
   F_RATES_ONLY = 16,              // reaction kernel: write total rates, no draw
-  F_CHECK_SKIN = 32
+  F_CHECK_SKIN = 32,
+  F_RX_NEXT = 64                  // drift kernel: copy the types forward and
+                                  // list the particles whose reaction draw of
+                                  // the next step may succeed
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------

@@ -2,9 +2,9 @@
 //
 // One handle = one CUDA stream + device buffers for a batch of independent
 // systems.  Set-up builds the flat tables (pair laws, walls, reactions,
-// bonded templates) and the tile decomposition; each rdsim_step launches,
-// per step: [EM] -> [rebuild every freq steps] -> [reactions] -> drift
-// (with the next step's EM fused in).
+// bonded templates), the cell grid and the CTA chunks of the list kernels;
+// each rdsim_step launches, per step: [EM] -> [rebuild (cells + Verlet list)
+// every freq steps] -> [reactions] -> drift (with the next step's EM fused in).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -69,8 +69,6 @@ struct rdsim_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
   int D = 2, nsys = 0, N = 0;
-  int tpp = 4, cap = 1024;
-  size_t dyn_smem = 0;
   int64_t step = 0;
   int freq = 10;
   bool has_rx = false;
@@ -78,9 +76,7 @@ struct rdsim_handle {
   int64_t device_bytes = 0;
   std::vector<HostSys> hs;
   std::vector<SysDev> sys_h;
-  std::vector<Tile> tiles_h;
   SysDev* sys_d = nullptr;
-  Tile* tiles_d = nullptr;
   PairLaw* laws_d = nullptr;
   WallLaw* walls_d = nullptr;
   RxDev* rx_d = nullptr;
@@ -89,12 +85,11 @@ struct rdsim_handle {
   int* atomterm_d = nullptr;
   int ncells = 0, nscan = 0;
   int *cell_count = nullptr, *cell_start = nullptr, *bsum = nullptr;
-  PlanCell* plan = nullptr;
-  PlanHead* plan_head = nullptr;
-  int plan_stride = 1;
   // Verlet-list kernels
-  bool list = true;
   int ltpp = 2;                      // lanes per particle
+  bool rx_pre = true;                // reaction prefilter (see rx_may_react)
+  int4* rx_list = nullptr;           // [2][npad] prefiltered particles
+  int* rx_count = nullptr;           // [2]
   int W = 0;                         // list width (entries per particle)
   int npad = 0;                      // particle stride of the list
   std::vector<Chunk> chunks_h;
@@ -200,7 +195,6 @@ Args make_args(rdsim_handle* h) {
   Args a;
   std::memset(&a, 0, sizeof a);
   a.sys = h->sys_d;
-  a.tiles = h->tiles_d;
   a.laws = h->laws_d;
   a.walls = h->walls_d;
   a.rx = h->rx_d;
@@ -208,9 +202,6 @@ Args make_args(rdsim_handle* h) {
   a.terms = h->terms_d;
   a.atomterm = h->atomterm_d;
   a.cell_start = h->cell_start;
-  a.plan = h->plan;
-  a.plan_head = h->plan_head;
-  a.plan_stride = h->plan_stride;
   for (int k = 0; k < 3; k++) {
     a.xh[k] = h->xh[h->cx][k];
     a.xl[k] = h->xl[h->cx][k];
@@ -226,8 +217,6 @@ Args make_args(rdsim_handle* h) {
   a.slot_of = h->slot_of;
   a.rates_out = h->rates;
   a.err = h->err;
-  a.ntiles = (int)h->tiles_h.size();
-  a.cap = h->cap;
   a.n_total = h->N;
   a.chunks = h->chunks_d;
   a.nbr = h->nbr;
@@ -235,30 +224,13 @@ Args make_args(rdsim_handle* h) {
   a.nbr_out = h->nbr;
   a.ncnt_out = h->ncnt;
   a.W = h->W;
+  a.rx_list = h->rx_list;
+  a.rx_count = h->rx_count;
+  a.sid = h->sid;
   a.npad = h->npad;
   a.single = h->nsys == 1 ? 1 : 0;
   if (!h->chunks_h.empty()) a.chunk1 = h->chunks_h[0];
   return a;
-}
-
-// The dynamic shared-memory limit is an attribute of the kernel on one device,
-// shared by every handle of the process: it is only ever raised, so that a
-// later handle with a smaller staging capacity does not invalidate the
-// launches of an earlier one.
-template <int D>
-int set_smem_attrs(int dev, size_t dyn) {
-  static std::mutex mu;
-  static std::map<int, size_t> have;
-  std::lock_guard<std::mutex> lock(mu);
-  size_t& cur = have[dev];
-  if (dyn <= cur) return 0;
-  if (cudaFuncSetAttribute(k_force<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess ||
-      cudaFuncSetAttribute(k_react<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess) {
-    cudaGetLastError();
-    return fail(RDSIM_ERR_CUDA, "cudaFuncSetAttribute(max dynamic shared memory) failed");
-  }
-  cur = dyn;
-  return 0;
 }
 
 template <int D, int TPP>
@@ -277,33 +249,26 @@ void launch_list_d(rdsim_handle* h, bool react, const Args& a) {
 }
 
 template <int D>
+void launch_listed(rdsim_handle* h, unsigned g, const Args& a) {
+  if (h->ltpp == 1) k_react_listed<D, 1><<<g, LBLOCK, 0, h->stream>>>(a);
+  else if (h->ltpp == 2) k_react_listed<D, 2><<<g, LBLOCK, 0, h->stream>>>(a);
+  else if (h->ltpp == 8) k_react_listed<D, 8><<<g, LBLOCK, 0, h->stream>>>(a);
+  else k_react_listed<D, 4><<<g, LBLOCK, 0, h->stream>>>(a);
+}
+
+template <int D>
 void launch_nlist(rdsim_handle* h, const Args& a) {
-  const dim3 grid((unsigned)h->chunks_h.size());
+  const dim3 grid((unsigned)(h->chunks_h.size() * (BUILD_LANES / h->ltpp)));
   if (h->ltpp == 1) k_nlist<D, 1><<<grid, LBLOCK, 0, h->stream>>>(a);
   else if (h->ltpp == 2) k_nlist<D, 2><<<grid, LBLOCK, 0, h->stream>>>(a);
   else if (h->ltpp == 8) k_nlist<D, 8><<<grid, LBLOCK, 0, h->stream>>>(a);
   else k_nlist<D, 4><<<grid, LBLOCK, 0, h->stream>>>(a);
 }
 
-void launch_tiles(rdsim_handle* h, bool react, const Args& a) {
-  if (h->list) {
-    if (h->D == 2) launch_list_d<2>(h, react, a);
-    else if (h->D == 3) launch_list_d<3>(h, react, a);
-    else launch_list_d<1>(h, react, a);
-    return;
-  }
-  if (h->tiles_h.empty()) return;
-  dim3 grid((unsigned)h->tiles_h.size());
-  if (h->D == 2) {
-    if (react) k_react<2><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-    else k_force<2><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-  } else if (h->D == 3) {
-    if (react) k_react<3><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-    else k_force<3><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-  } else {
-    if (react) k_react<1><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-    else k_force<1><<<grid, BLOCK, h->dyn_smem, h->stream>>>(a);
-  }
+void launch_step_kernel(rdsim_handle* h, bool react, const Args& a) {
+  if (h->D == 2) launch_list_d<2>(h, react, a);
+  else if (h->D == 3) launch_list_d<3>(h, react, a);
+  else launch_list_d<1>(h, react, a);
 }
 
 unsigned nblk(int n, int b = 256) { return (unsigned)((n + b - 1) / b); }
@@ -331,26 +296,13 @@ int rebuild(rdsim_handle* h) {
   if (h->D == 2) k_order<2><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
   else if (h->D == 3) k_order<3><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
   else k_order<1><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
-  if (h->list) {
-    h->cx = 1 - h->cx;
-    h->cm = 1 - h->cm;
-    h->co = 1 - h->co;
-    const Args b = make_args(h);
-    if (h->D == 2) launch_nlist<2>(h, b);
-    else if (h->D == 3) launch_nlist<3>(h, b);
-    else launch_nlist<1>(h, b);
-    CK(cudaGetLastError());
-    return 0;
-  }
-  if (!h->tiles_h.empty()) {
-    const unsigned nt = (unsigned)h->tiles_h.size();
-    if (h->D == 2) k_plan<2><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
-    else if (h->D == 3) k_plan<3><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
-    else k_plan<1><<<nt, BLOCK, 0, h->stream>>>(h->sys_d, h->tiles_d, h->cell_start, h->plan, h->plan_head, h->plan_stride);
-  }
   h->cx = 1 - h->cx;
   h->cm = 1 - h->cm;
   h->co = 1 - h->co;
+  const Args b = make_args(h);
+  if (h->D == 2) launch_nlist<2>(h, b);
+  else if (h->D == 3) launch_nlist<3>(h, b);
+  else launch_nlist<1>(h, b);
   CK(cudaGetLastError());
   return 0;
 }
@@ -365,15 +317,17 @@ int force(rdsim_handle* h, long long step, int flags, const double* xi_next, boo
   a.xi = xi_next;
   {
     ProfScope ps(h, P_FORCE, 1);
-    launch_tiles(h, false, a);
+    launch_step_kernel(h, false, a);
   }
   CK(cudaGetLastError());
   if (flags & F_EM) h->cx = 1 - h->cx;
   return 0;
 }
 
+// `listed`: the previous drift kernel copied the types forward and listed
+// the particles whose draw may succeed; only those are processed.
 int react(rdsim_handle* h, long long step, int flags, const double* u1, const double* u2,
-          bool rel = false) {
+          bool rel = false, bool listed = false) {
   Args a = make_args(h);
   a.step_base = rel ? h->step_dev : nullptr;
   a.step = step;
@@ -382,7 +336,14 @@ int react(rdsim_handle* h, long long step, int flags, const double* u1, const do
   a.u2 = u2;
   {
     ProfScope ps(h, (flags & F_RATES_ONLY) ? P_HOOK : P_REACT, 1);
-    launch_tiles(h, true, a);
+    if (listed) {
+      const unsigned g = (unsigned)std::min(2 * 152, (h->N + 3) / 4);
+      if (h->D == 2) launch_listed<2>(h, g, a);
+      else if (h->D == 3) launch_listed<3>(h, g, a);
+      else launch_listed<1>(h, g, a);
+    } else {
+      launch_step_kernel(h, true, a);
+    }
   }
   CK(cudaGetLastError());
   if (!(flags & F_RATES_ONLY)) h->cm = 1 - h->cm;
@@ -522,7 +483,7 @@ bool snapshot_in(rdsim_handle* h, long long a, long long b) {
 // update of the next step) as a CUDA graph.  Graphs are cached per buffer
 // parity state; kernel step numbers are offsets from a device counter that
 // the graph advances by freq at its end.
-int run_period_graph(rdsim_handle* h, long long s, int kf) {
+int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
   const int key = h->cx | (h->cm << 1) | (h->co << 2) | ((kf & F_NO_NOISE) ? 8 : 0);
   auto it = h->graph_cache.find(key);
   const int cx0 = h->cx, cm0 = h->cm, co0 = h->co;
@@ -533,8 +494,10 @@ int run_period_graph(rdsim_handle* h, long long s, int kf) {
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int rc = rebuild(h);
     for (int i = 0; i < h->freq && !rc; i++) {
-      if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true);
-      if (!rc) rc = force(h, i, F_EM | kf, nullptr, true);
+      // the prefilter flags of step i come from the drift kernel of step i - 1
+      const bool flagged = pre && i > 0, flag_next = pre && i + 1 < h->freq;
+      if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
+      if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
     }
     if (!rc) k_set_counter<<<1, 1, 0, h->stream>>>(h->step_dev, h->freq, 1);
     cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
@@ -573,10 +536,10 @@ void free_all(rdsim_handle* h) {
   auto F = [](void* p) {
     if (p) cudaFree(p);
   };
-  F(h->sys_d); F(h->tiles_d); F(h->laws_d); F(h->walls_d); F(h->rx_d); F(h->tmpl_d);
+  F(h->sys_d); F(h->laws_d); F(h->walls_d); F(h->rx_d); F(h->tmpl_d);
   F(h->terms_d); F(h->atomterm_d); F(h->cell_count); F(h->cell_start); F(h->bsum);
   F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
-  F(h->plan); F(h->plan_head); F(h->chunks_d); F(h->nbr); F(h->ncnt);
+  F(h->chunks_d); F(h->nbr); F(h->ncnt); F(h->rx_list); F(h->rx_count);
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
@@ -595,8 +558,13 @@ void free_all(rdsim_handle* h) {
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
-float guard2(double r, double unit) {  // half-width of the r^2 guard band
-  return (float)(r * r * 1e-5 + 2.0 * r * 4.0 * unit + 1e-12);
+// Half-width of the guard band around r^2 inside which the float64 distance
+// decides.  The kernels' float32 r^2 from high words errs by less than
+// 5e-7 r^2 (rounding of the unit, the conversion, the products and the sum)
+// plus 2 r sqrt(3) unit (truncation of both coordinates); the band is four
+// times wider.
+float guard2(double r, double unit) {
+  return (float)(r * r * 2e-6 + 2.0 * r * 4.0 * unit + 1e-12);
 }
 
 }  // namespace
@@ -615,7 +583,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   h->device = opt.device;
   h->D = systems[0].n_dim;
   h->nsys = n_systems;
-  h->tpp = 32;  // the pair loops run one warp per particle
   int rc = 0;
   auto bail = [&](int code) {
     free_all(h);
@@ -639,11 +606,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   std::vector<int> sid_h;
   int total_cells = 0;
   double skin_report = 0, cell_report = 1e300, range_report = 0;
-  int target = opt.tile_target > 0 ? opt.tile_target : 56;
-  {
-    const char* alg = std::getenv("RDSIM_TILES");
-    h->list = !(alg && alg[0] == '1');
-  }
+  bool rx_pre_worth = true;  // few draws expected to pass the bound
   if (opt.threads_per_particle == 1 || opt.threads_per_particle == 2 ||
       opt.threads_per_particle == 4 || opt.threads_per_particle == 8)
     h->ltpp = opt.threads_per_particle;
@@ -816,7 +779,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         for (auto& L : v) {
           laws.push_back(L);
           R2 = std::max(R2, L.rc2_hi);
+          sd.prc2[a * MAXT + b] = std::max(sd.prc2[a * MAXT + b], L.rc2_hi);
         }
+        sd.prc2[b * MAXT + a] = sd.prc2[a * MAXT + b];
         unsigned short code = (unsigned short)((first << 5) | (int)v.size());
         sd.ppair[a * MAXT + b] = code;
         sd.ppair[b * MAXT + a] = code;
@@ -864,6 +829,11 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         }
       }
       sd.rx_any_mask |= 1 << r.reactant;
+      if (r.kind == RDSIM_RX_CATALYZED) sd.rxB[r.reactant] += r.rate;
+      else sd.rxA[r.reactant] += r.rate;  // linear; inhibited at most its rate
+      if (!(r.rate >= 0.0 && std::isfinite(r.rate)) ||
+          (r.kind == RDSIM_RX_INHIBITED && !(r.rate_decrease >= 0.0)))
+        h->rx_pre = false;  // the bound needs non-negative rates
       rxs.push_back(x);
     }
     sd.nrx = S.n_reactions;
@@ -877,7 +847,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     double skin = opt.skin > 0 ? opt.skin : 10.0 * sig * std::sqrt((double)h->freq) + 0.05 * R + 0.1;
     double delta = skin / 2;
     if (R > 0) {
-      double room = (S.rs - R) / (2.0 * std::sqrt((double)D));
+      double room = (S.rs - R) / 2.0;
       if (room <= 1e-6 * R)
         return bail(fail(RDSIM_ERR_UNSUPPORTED,
                          "rs must exceed the largest interaction / reaction range"));
@@ -889,14 +859,18 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     // with no pair work the displacement check is off
     sd.delta = R > 0 ? (float)delta : 1e30f;
     // Verlet-list radius: a pair within range at some step of a rebuild period
-    // was within range + 2 sqrt(D) delta at its start (plus float margin)
+    // was within range + 2 delta at its start (plus float margin)
     if (R > 0) {
-      const double rr = std::sqrt((double)std::max(R2, Rrx2)) + 2.0 * std::sqrt((double)D) * delta;
+      const double rr = std::sqrt((double)std::max(R2, Rrx2)) + 2.0 * delta;
       const double rl = rr * (1.0 + 1e-6) + 8.0 * max_unit;
       sd.Rl2 = (float)(rl * rl);
       double vol = 1.0, ball = D == 1 ? 2.0 * rl : (D == 2 ? M_PI * rl * rl : 4.0 / 3.0 * M_PI * rl * rl * rl);
       for (int k = 0; k < D; k++) vol *= S.L[k];
-      list_expect = std::max(list_expect, std::min((double)S.n_particles, S.n_particles / vol * ball));
+      const double expect = std::min((double)S.n_particles, S.n_particles / vol * ball);
+      list_expect = std::max(list_expect, expect);
+      // the prefilter pays when few draws can succeed
+      for (int t = 0; t < MAXT; t++)
+        if (S.dt * (sd.rxA[t] + sd.rxB[t] * expect) > 0.02) rx_pre_worth = false;
     }
     // cells
     int ncs = 1;
@@ -918,63 +892,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     sd.c0 = total_cells;
     total_cells += ncs;
     if (total_cells < 0 || total_cells > (1 << 28)) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many cells"));
-    // tiles
-    double per_cell = (double)S.n_particles / ncs;
-    double cells_per_tile = std::max(1.0, target / std::max(per_cell, 1e-9));
-    int w[3] = {1, 1, 1};
-    double side = std::pow(cells_per_tile, 1.0 / D);
-    for (int k = 0; k < D; k++) {
-      int wk = std::max(1, (int)std::lround(side));
-      int lim = sd.nc[k];
-      if (((sd.periodic >> k) & 1) && sd.nc[k] >= 3) lim = sd.nc[k] - 2;
-      if (sd.nc[k] == 1) lim = 1;
-      wk = std::min(wk, lim);
-      w[k] = wk;
-    }
-    auto halo_cells = [&]() {
-      int p = 1;
-      for (int k = 0; k < D; k++) p *= w[k] + 2 * sd.halo[k];
-      return p;
-    };
-    while (halo_cells() > MAXHC) {
-      int kk = 0;
-      for (int k = 1; k < D; k++)
-        if (w[k] > w[kk]) kk = k;
-      if (w[kk] == 1) break;
-      w[kk]--;
-    }
-    if (halo_cells() > MAXHC) return bail(fail(RDSIM_ERR_UNSUPPORTED, "tile halo too large"));
-    sd.ntile0 = (int)h->tiles_h.size();
-    int nt[3] = {1, 1, 1};
-    for (int k = 0; k < D; k++) nt[k] = (sd.nc[k] + w[k] - 1) / w[k];
-    for (int tz = 0; tz < nt[2]; tz++)
-      for (int ty = 0; ty < nt[1]; ty++)
-        for (int tx = 0; tx < nt[0]; tx++) {
-          Tile t;
-          std::memset(&t, 0, sizeof t);
-          t.sys = si;
-          int tt[3] = {tx, ty, tz};
-          t.nhc = 1;
-          for (int k = 0; k < 3; k++) {
-            t.w[k] = 1;
-            t.hdim[k] = 1;
-          }
-          for (int k = 0; k < D; k++) {
-            t.c[k] = tt[k] * w[k];
-            t.w[k] = std::min(w[k], sd.nc[k] - t.c[k]);
-            t.hdim[k] = t.w[k] + 2 * sd.halo[k];
-            t.nhc *= t.hdim[k];
-          }
-          t.law0 = sd.law0;
-          t.nlaws = sd.nlaws;
-          t.wall0 = sd.wall0;
-          t.nwalls = sd.nwalls;
-          t.rx0 = sd.rx0;
-          t.nrx = sd.nrx;
-          h->plan_stride = std::max(h->plan_stride, t.nhc);
-          h->tiles_h.push_back(t);
-        }
-    sd.ntiles = (int)h->tiles_h.size() - sd.ntile0;
     // bonded templates
     std::map<int, int> tmpl_index;  // molecule_id -> device template
     std::vector<int> tmpl_of_mol(S.n_molecules, 0xff);
@@ -1095,26 +1012,10 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   h->range = range_report;
   h->ncells = total_cells;
   h->nscan = std::max(1, (total_cells + SCAN_TILE - 1) / SCAN_TILE);
-  // staging capacity from the expected halo population (x4 margin)
-  {
-    double worst = 0;
-    for (const SysDev& sd : h->sys_h) {
-      int ncs = 1;
-      for (int k = 0; k < D; k++) ncs *= sd.nc[k];
-      const Tile& t = h->tiles_h[sd.ntile0];
-      int hc = 1;
-      for (int k = 0; k < D; k++) hc *= t.w[k] + 2 * sd.halo[k];
-      worst = std::max(worst, 2.5 * hc * (double)sd.n / ncs);
-    }
-    int cap = (int)std::ceil(worst / 256.0) * 256;
-    h->cap = std::max(256, std::min(4096, cap));
-    // staged records (4 words), sorted index, mol (D == 3), own index, and
-    // per-own-particle force (D words) or packed reaction counters (4 words)
-    h->dyn_smem = (size_t)h->cap * (7 + std::max(D, MAXR / 2)) * 4;
-  }
+  if (opt.reaction_prefilter < 0 || (opt.reaction_prefilter == 0 && !rx_pre_worth)) h->rx_pre = false;
   // list kernels: CTA chunks per system; list width from the expected
   // population (rows beyond it are regenerated from the cells)
-  if (h->list) {
+  {
     const int per = LBLOCK / h->ltpp;
     for (int si = 0; si < (int)h->sys_h.size(); si++) {
       const SysDev& sd = h->sys_h[si];
@@ -1147,7 +1048,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   int64_t& B = h->device_bytes;
   const int N = h->N;
   if ((rc = dalloc(&h->sys_d, h->sys_h.size(), &B))) return bail(rc);
-  if ((rc = dalloc(&h->tiles_d, h->tiles_h.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->laws_d, laws.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->walls_d, walls.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->rx_d, rxs.size(), &B))) return bail(rc);
@@ -1156,8 +1056,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->atomterm_d, atomterm.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_count, (size_t)h->ncells, &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_start, (size_t)h->ncells + 1, &B))) return bail(rc);
-  if ((rc = dalloc(&h->plan, h->tiles_h.size() * (size_t)h->plan_stride, &B))) return bail(rc);
-  if ((rc = dalloc(&h->plan_head, h->tiles_h.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->bsum, (size_t)h->nscan, &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_of, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->rank_of, N, &B))) return bail(rc);
@@ -1182,10 +1080,14 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->tbuf, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->err, 1, &B))) return bail(rc);
   if ((rc = dalloc(&h->step_dev, 1, &B))) return bail(rc);
-  if (h->list) {
+  {
     if ((rc = dalloc(&h->chunks_d, h->chunks_h.size(), &B))) return bail(rc);
     if ((rc = dalloc(&h->nbr, (size_t)h->W * h->npad, &B))) return bail(rc);
     if ((rc = dalloc(&h->ncnt, N, &B))) return bail(rc);
+    if ((rc = dalloc(&h->rx_list, 2 * (size_t)h->npad, &B))) return bail(rc);
+    if ((rc = dalloc(&h->rx_count, 2, &B))) return bail(rc);
+    if (cudaMemsetAsync(h->rx_count, 0, 2 * sizeof(int), h->stream) != cudaSuccess)
+      return bail(fail(RDSIM_ERR_CUDA, "memset"));
   }
   h->graphs = opt.use_graphs >= 0;
   if ((rc = dalloc(&h->cl_d, (size_t)3 * h->nsys, &B))) return bail(rc);
@@ -1198,8 +1100,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   for (int s = 0; s < h->nsys; s++)
     for (int k = 0; k < D; k++) cl[3 * s + k] = h->hs[s].cl_ref[k];
   if ((rc = up(h->sys_d, h->sys_h.data(), sizeof(SysDev) * h->sys_h.size()))) return bail(rc);
-  if ((rc = up(h->tiles_d, h->tiles_h.data(), sizeof(Tile) * h->tiles_h.size()))) return bail(rc);
-  if (h->list && (rc = up(h->chunks_d, h->chunks_h.data(), sizeof(Chunk) * h->chunks_h.size())))
+  if ((rc = up(h->chunks_d, h->chunks_h.data(), sizeof(Chunk) * h->chunks_h.size())))
     return bail(rc);
   if ((rc = up(h->laws_d, laws.data(), sizeof(PairLaw) * laws.size()))) return bail(rc);
   if ((rc = up(h->walls_d, walls.data(), sizeof(WallLaw) * walls.size()))) return bail(rc);
@@ -1214,10 +1115,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   for (int k = 0; k < D; k++)
     if (cudaMemsetAsync(h->drift[k], 0, sizeof(float) * N, h->stream) != cudaSuccess)
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
-  if (D == 2) rc = set_smem_attrs<2>(h->device, h->dyn_smem);
-  else if (D == 3) rc = set_smem_attrs<3>(h->device, h->dyn_smem);
-  else rc = set_smem_attrs<1>(h->device, h->dyn_smem);
-  if (rc) return bail(rc);
   if ((rc = upload_state(h, x_all, t_all))) return bail(rc);
   if ((rc = initial_drift(h))) return bail(rc);
   *out = h;
@@ -1279,21 +1176,26 @@ int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi
   // first step: the stand-alone update with the drift left by the last call
   if ((rc = em(h, h->step + 1, kf, dxi))) return rc;
   const bool graphable = h->graphs && !inj && !h->prof;
+  // reaction prefilter: needs the counter-based draws (not injected ones)
+  const bool pre = h->rx_pre && h->has_rx && !inj;
+  bool flagged = false;  // the last drift kernel flagged this step's draws
   for (int q = 0; q < n_steps;) {
     const long long s = h->step + 1;
     const int left = n_steps - q;
     if (graphable && s % h->freq == 0 && left > h->freq && !snapshot_in(h, s, s + h->freq - 1)) {
-      if ((rc = run_period_graph(h, s, kf))) return rc;
+      if ((rc = run_period_graph(h, s, kf, pre))) return rc;
       h->step = s + h->freq - 1;
       q += h->freq;
+      flagged = false;
       continue;
     }
     if (s % h->freq == 0) {
       if ((rc = rebuild(h))) return rc;
+      flagged = false;  // flags are in the order before the re-sort
     }
     if (h->has_rx) {
       if ((rc = react(h, s, kf, du1 ? du1 + (size_t)q * N : nullptr,
-                      du2 ? du2 + (size_t)q * N : nullptr)))
+                      du2 ? du2 + (size_t)q * N : nullptr, false, flagged)))
         return rc;
     }
     if (h->traj_frames > 0 && s % h->traj_stride == 0) {
@@ -1302,7 +1204,9 @@ int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi
     }
     const bool last = q == n_steps - 1;
     const double* xn = (dxi && !last) ? dxi + (size_t)(q + 1) * N * D : nullptr;
-    if ((rc = force(h, s, last ? F_STORE_DRIFT | kf : F_EM | kf, xn))) return rc;
+    flagged = pre && !last && (s + 1) % h->freq != 0;
+    if ((rc = force(h, s, (last ? F_STORE_DRIFT : F_EM) | kf | (flagged ? F_RX_NEXT : 0), xn)))
+      return rc;
     h->step = s;
     q++;
   }
@@ -1528,13 +1432,14 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
   std::memset(info, 0, sizeof *info);
   info->n_particles = h->N;
   info->n_cells = h->ncells;
-  info->n_tiles = h->list ? (int64_t)h->chunks_h.size() : (int64_t)h->tiles_h.size();
-  info->threads_per_particle = h->list ? h->ltpp : h->tpp;
-  info->max_tile_particles = h->list ? h->W : h->cap;
+  info->n_blocks = (int64_t)h->chunks_h.size();
+  info->threads_per_particle = h->ltpp;
+  info->list_width = h->W;
   info->skin = h->skin;
   info->cell_size_min = h->cell_min;
   info->interaction_range = h->range;
   info->device_bytes = h->device_bytes;
+  info->reaction_prefilter = (h->rx_pre && h->has_rx) ? 1 : 0;
   return 0;
 }
 

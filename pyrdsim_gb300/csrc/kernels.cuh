@@ -1,34 +1,17 @@
-// kernels.cuh -- sm_103a kernels of the simulation step.
+// kernels.cuh -- sm_103a device code of the simulation step shared by the
+// list kernels (list.cuh): pair laws, walls, bonded terms, Euler-Maruyama
+// update, reaction propensities and draws, and the cell-list rebuild.
 //
 //   k_bin / k_scan_* / k_scatter / k_order : cell-list rebuild, a warp-
 //       aggregated counting sort of all systems' particles into cells
 //       (replaces create_neighbor_list, pyrdsim.pyx:1448-1587)
-//   k_react<D,TPP>  : neighbourhood-dependent reaction propensities and the
-//       draws that flip particle types (reaction_step, pyrdsim.pyx:2070-2223)
-//   k_force<D,TPP>  : pair + wall + bonded drift (update_drifts,
-//       pyrdsim.pyx:1941-2067), optionally fused with the next step's
-//       Euler-Maruyama update and boundary conditions (pyrdsim.pyx:2225-2292)
 //   k_em<D>         : stand-alone Euler-Maruyama update
 //   hooks           : reference cell ids, neighbour pairs, snapshots
-//
-// Tile kernels: one CTA per tile of cells of one system.  The CTA stages the
-// tile plus a one-cell halo (cell-sorted, so every halo row of cells is one
-// contiguous range) into shared memory, then TPP threads share each own
-// particle's candidate loop and combine with warp shuffles.  If a tile's
-// halo exceeds the shared-memory capacity the same loop reads global memory.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include "device.cuh"
-
-// resident CTAs per SM each tile kernel is compiled for (register budget)
-#ifndef RD_FORCE_MIN_BLOCKS
-#define RD_FORCE_MIN_BLOCKS 8
-#endif
-#ifndef RD_REACT_MIN_BLOCKS
-#define RD_REACT_MIN_BLOCKS 8
-#endif
 
 namespace rd {
 
@@ -80,7 +63,10 @@ __device__ double exact_dist(const SysDev& s, const Args& a, int gi, int gj) {
     double xi = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
     double xj = fixed_to_double(s, k, a.xh[k][gj], a.xl[k][gj]);
     double v = __dsub_rn(xj, xi);
-    if ((s.periodic >> k) & 1) v = __dsub_rn(v, __dmul_rn(s.L[k], round(__ddiv_rn(v, s.L[k]))));
+    // minimum image; round(v / L) is 0 whenever |v| < 0.49 L, which holds for
+    // every pair of adjacent cells except in boxes of three cells or fewer
+    if (((s.periodic >> k) & 1) && !(fabs(v) < 0.49 * s.L[k]))
+      v = __dsub_rn(v, __dmul_rn(s.L[k], round(__ddiv_rn(v, s.L[k]))));
     d2 = __dadd_rn(d2, __dmul_rn(v, v));
   }
   return __dsqrt_rn(d2);
@@ -129,7 +115,7 @@ template <int D>
 __device__ inline float pair_force(const SysDev& s, const PairLaw* laws, const Args& a, int gi,
                                    int gj, unsigned int pp, float r2) {
   const int nl = pp & 31, l0 = pp >> 5;
-  const float inv_r2 = __frcp_rn(r2);
+  const float inv_r2 = __fdividef(1.0f, r2);
   float fr = 0.f;
   double dexact = -1.0;
   for (int l = l0; l < l0 + nl; l++) {
@@ -151,201 +137,29 @@ __device__ inline float pair_force(const SysDev& s, const PairLaw* laws, const A
   return fr;
 }
 
-// ---------------------------------------------------------------------------
-// Block-wide exclusive scan of MAXHC ints held two per thread (BLOCK = 128).
-__device__ inline void scan_pairs(int* v, int* warp_tmp, int* total) {
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  int a0 = v[2 * tid], a1 = v[2 * tid + 1];
-  int s = a0 + a1, inc = s;
+// Block-wide copies of words from global to shared memory (blockDim.x ==
+// BLOCK).  All loads are issued before any store: through generic pointers
+// the compiler could not otherwise move a load past the previous iteration's
+// store, and every iteration would wait a full memory round trip.
+template <int MAXN>
+struct WordLoad {
+  static constexpr int IT = MAXN > 0 ? (MAXN + BLOCK - 1) / BLOCK : 1;
+  int v[IT];
+  __device__ inline void load(const int* __restrict__ src, int n) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) warp_tmp[w] = inc;
-  __syncthreads();
-  int off = 0;
-  for (int q = 0; q < w; q++) off += warp_tmp[q];
-  int ex = off + inc - s;
-  if (tid == BLOCK - 1) *total = ex + s;
-  __syncthreads();
-  v[2 * tid] = ex;
-  v[2 * tid + 1] = ex + a0;
-  __syncthreads();
-}
-
-// last index q in [0, n) with arr[q] <= key (arr non-decreasing, arr[0] <= key)
-__device__ inline int last_le(const int* arr, int n, int key) {
-  int lo = 0, hi = n;  // answer in [lo, hi)
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (arr[mid] <= key) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-template <int D>
-struct TileShared {
-  SysDev sys;
-  PairLaw laws[MAXI];
-  WallLaw walls[MAXW];
-  RxDev rx[MAXR];
-  PlanCell pc[MAXHC];
-  int hdim[3];
-  int nhc, total, nown, use_smem;
-};
-
-// Staged halo particles: one 16-byte record each.  D <= 2: {x0, x1, meta,
-// mol}; D == 3: {x0, x1, x2, meta} with mol in a separate array.  sgi holds
-// the particle's index in the sorted global arrays.
-template <int D>
-struct Staged {
-  uint4* sp;
-  int* smol;
-  int* sgi;
-};
-
-__device__ inline void copy_words(int* dst, const int* src, int n) {
-  for (int q = threadIdx.x; q < n; q += BLOCK) dst[q] = src[q];
-}
-
-// Load the system, its tables and the tile's plan (one round trip), then
-// gather the halo particles into shared memory (a second one).
-template <int D>
-__device__ Staged<D> tile_setup(TileShared<D>& sh, const Args& a, const Tile& t,
-                                uint32_t* dyn) {
-  const int tid = threadIdx.x;
-  copy_words(reinterpret_cast<int*>(&sh.sys), reinterpret_cast<const int*>(&a.sys[t.sys]),
-             (int)(sizeof(SysDev) / 4));
-  copy_words(reinterpret_cast<int*>(sh.laws), reinterpret_cast<const int*>(a.laws + t.law0),
-             t.nlaws * (int)(sizeof(PairLaw) / 4));
-  copy_words(reinterpret_cast<int*>(sh.walls), reinterpret_cast<const int*>(a.walls + t.wall0),
-             t.nwalls * (int)(sizeof(WallLaw) / 4));
-  copy_words(reinterpret_cast<int*>(sh.rx), reinterpret_cast<const int*>(a.rx + t.rx0),
-             t.nrx * (int)(sizeof(RxDev) / 4));
-  copy_words(reinterpret_cast<int*>(sh.pc),
-             reinterpret_cast<const int*>(a.plan + (size_t)blockIdx.x * a.plan_stride),
-             t.nhc * 4);
-  if (tid == 0) {
-    const PlanHead hd = a.plan_head[blockIdx.x];
-    sh.total = hd.total;
-    sh.nown = hd.nown;
-    sh.nhc = t.nhc;
-    for (int k = 0; k < 3; k++) sh.hdim[k] = t.hdim[k];
-    sh.use_smem = hd.total <= a.cap ? 1 : 0;
-  }
-  __syncthreads();
-  Staged<D> st;
-  st.sp = reinterpret_cast<uint4*>(dyn);
-  st.sgi = reinterpret_cast<int*>(dyn + 4 * a.cap);
-  st.smol = reinterpret_cast<int*>(dyn + 5 * a.cap);
-  if (sh.use_smem) {
-    const int total = sh.total, nhc = sh.nhc;
-    for (int e = tid; e < total; e += BLOCK) {
-      int lo = 0, hi = nhc;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (sh.pc[mid].beg <= e) lo = mid;
-        else hi = mid;
-      }
-      const int src = sh.pc[lo].gbeg + (e - sh.pc[lo].beg);
-      uint4 v;
-      v.x = a.xh[0][src];
-      v.y = D > 1 ? a.xh[1][src] : 0u;
-      if (D == 3) {
-        v.z = a.xh[2][src];
-        v.w = a.meta[src];
-        st.smol[e] = a.mol[src];
-      } else {
-        v.z = a.meta[src];
-        v.w = (uint32_t)a.mol[src];
-      }
-      st.sp[e] = v;
-      st.sgi[e] = src;
+    for (int u = 0; u < IT; u++) {
+      const int q = (int)threadIdx.x + u * BLOCK;
+      v[u] = q < n ? __ldg(src + q) : 0;
     }
   }
-  __syncthreads();
-  return st;
-}
-
-// Candidate data by index: shared records, or the global arrays when the
-// halo did not fit.
-template <int D, bool SMEM>
-__device__ inline void cand(const Staged<D>& st, const Args& a, int j, uint32_t* x,
-                            uint32_t& meta, int& mol) {
-  if (SMEM) {
-    const uint4 v = st.sp[j];
-    x[0] = v.x;
-    if (D > 1) x[1] = v.y;
-    if (D == 3) {
-      x[2] = v.z;
-      meta = v.w;
-      mol = st.smol[j];
-    } else {
-      meta = v.z;
-      mol = (int)v.w;
-    }
-  } else {
+  __device__ inline void store(int* __restrict__ dst, int n) const {
 #pragma unroll
-    for (int k = 0; k < D; k++) x[k] = a.xh[k][j];
-    meta = a.meta[j];
-    mol = a.mol[j];
-  }
-}
-
-template <int D, bool SMEM>
-__device__ inline int cand_gi(const Staged<D>& st, int j) {
-  return SMEM ? st.sgi[j] : j;
-}
-
-// Source index of own particle p (exclusive prefix of interior counts).
-template <bool SMEM>
-__device__ inline int own_index(const PlanCell* pc, int nhc, int p, int* qout) {
-  int lo = 0, hi = nhc;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (pc[mid].own <= p) lo = mid;
-    else hi = mid;
-  }
-  *qout = lo;
-  return (SMEM ? pc[lo].beg : pc[lo].gbeg) + (p - pc[lo].own);
-}
-
-// Visit every candidate neighbour of an own particle in halo cell q: the
-// 3^D (or fewer) cells around it; fn(j) gets the source index.
-template <int D, int TPP, bool SMEM, class Fn>
-__device__ inline void for_candidates(const TileShared<D>& sh, int q, int lane_g, Fn&& fn) {
-  const SysDev& s = sh.sys;
-  int hc[3] = {0, 0, 0};
-  {
-    int rem = q;
-    for (int k = 0; k < D; k++) {
-      hc[k] = rem % sh.hdim[k];
-      rem /= sh.hdim[k];
+    for (int u = 0; u < IT; u++) {
+      const int q = (int)threadIdx.x + u * BLOCK;
+      if (q < n) dst[q] = v[u];
     }
   }
-  const int h0 = s.halo[0];
-  const int h1 = D > 1 ? s.halo[1] : 0;
-  const int h2 = D > 2 ? s.halo[2] : 0;
-  for (int dz = -h2; dz <= h2; dz++) {
-    for (int dy = -h1; dy <= h1; dy++) {
-      int rowbase = 0;
-      if (D == 2) rowbase = (hc[1] + dy) * sh.hdim[0];
-      if (D == 3) rowbase = ((hc[2] + dz) * sh.hdim[1] + (hc[1] + dy)) * sh.hdim[0];
-      const int qa = rowbase + hc[0] - h0, qb = rowbase + hc[0] + h0;
-      if (SMEM) {
-        const int b = sh.pc[qa].beg, e = sh.pc[qb].beg + sh.pc[qb].cnt;
-        for (int j = b + lane_g; j < e; j += TPP) fn(j);
-      } else {
-        for (int qq = qa; qq <= qb; qq++) {
-          const int b = sh.pc[qq].gbeg, e = b + sh.pc[qq].cnt;
-          for (int j = b + lane_g; j < e; j += TPP) fn(j);
-        }
-      }
-    }
-  }
-}
+};
 
 __device__ inline long long delta_fixed(float d, float inv_unit_hi, bool* bad) {
   float v = d * inv_unit_hi;
@@ -553,113 +367,23 @@ __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const A
     if (!isfinite(acc[k])) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)acc[k], eff_step(a));
   if (a.flags & F_CHECK_SKIN) {
     // displacement since the last rebuild: keeps every pair within range in
-    // adjacent cells and within rs of each other at that rebuild
+    // adjacent cells, in the Verlet list and within rs of each other at that
+    // rebuild
+    float rel2 = 0.f;
 #pragma unroll
     for (int k = 0; k < D; k++) {
-      const float rel = fabsf((float)(int)(xo_h[k] - a.xr[k][gi])) * s.unit_hi[k];
-      if (rel > s.delta) record_error(a.err, RDSIM_ERR_SKIN, pid, k, (double)rel, eff_step(a));
+      const float rel = (float)(int)(xo_h[k] - a.xr[k][gi]) * s.unit_hi[k];
+      rel2 += rel * rel;
     }
+    if (rel2 > s.delta * s.delta)
+      record_error(a.err, RDSIM_ERR_SKIN, pid, -1, (double)sqrtf(rel2), eff_step(a));
   }
   if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags);
 }
 
-// Drift kernel.  Phase A: TPP threads per own particle run the pair loop and
-// combine with shuffles into shared memory.  Phase B: one thread per own
-// particle adds walls and bonded terms, stores the drift and/or performs the
-// fused Euler-Maruyama update, so no lane idles in the per-particle tail.
-template <int D, int TPP, bool SMEM>
-__device__ void force_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a,
-                           uint32_t* dyn) {
-  const SysDev& s = sh.sys;
-  int* oidx = reinterpret_cast<int*>(dyn + 6 * a.cap);
-  float* ofr = reinterpret_cast<float*>(dyn + 7 * a.cap);
-  const int tid = threadIdx.x;
-  const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
-  const int nhc = sh.nhc, nown = sh.nown;
-  float unit[3];
-#pragma unroll
-  for (int k = 0; k < D; k++) unit[k] = s.unit_hi[k];
-  const float R2 = s.R2;
-  for (int base = 0; base < nown; base += a.cap) {
-    const int nch = min(a.cap, nown - base);
-    for (int p0 = 0; p0 < nch; p0 += groups) {
-      const int pl = p0 + g;
-      const bool active = pl < nch;
-      float acc[3] = {0.f, 0.f, 0.f};
-      int idx = 0;
-      if (active) {
-        int q;
-        idx = own_index<SMEM>(sh.pc, nhc, base + pl, &q);
-        const int gi = cand_gi<D, SMEM>(st, idx);
-        uint32_t xi_h[3] = {0u, 0u, 0u}, mi;
-        int moli;
-        cand<D, SMEM>(st, a, idx, xi_h, mi, moli);
-        const int ti = mi & 0xff, trbi = (mi >> 8) & 0xff;
-        const unsigned int pmask = s.partner[trbi];
-        if (R2 > 0.f) for_candidates<D, TPP, SMEM>(sh, q, lane_g, [&](int j) {
-          uint32_t xj[3] = {0u, 0u, 0u}, mj;
-          int molj;
-          cand<D, SMEM>(st, a, j, xj, mj, molj);
-          float dx[3], r2 = 0.f;
-#pragma unroll
-          for (int k = 0; k < D; k++) {
-            dx[k] = (float)(int)(xj[k] - xi_h[k]) * unit[k];
-            r2 += dx[k] * dx[k];
-          }
-          if (!(r2 < R2)) return;
-          if (molj == moli) return;  // same molecule (and self)
-          const int tj = mj & 0xff, trbj = (mj >> 8) & 0xff;
-          if (!((pmask >> trbj) & 1)) return;
-          const unsigned int pp = s.ppair[ti * MAXT + tj];
-          if (!(pp & 31)) return;
-          const float fr = pair_force<D>(s, sh.laws, a, gi, cand_gi<D, SMEM>(st, j), pp, r2);
-#pragma unroll
-          for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
-        });
-      }
-#pragma unroll
-      for (int o = TPP >> 1; o > 0; o >>= 1) {
-#pragma unroll
-        for (int k = 0; k < D; k++) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-      }
-      if (active && lane_g == 0) {
-        oidx[pl] = idx;
-#pragma unroll
-        for (int k = 0; k < D; k++) ofr[k * a.cap + pl] = acc[k];
-      }
-    }
-    __syncthreads();
-    for (int pl = tid; pl < nch; pl += BLOCK) {
-      const int idx = oidx[pl];
-      const int gi = cand_gi<D, SMEM>(st, idx);
-      uint32_t xo_h[3] = {0u, 0u, 0u}, mi;
-      int moli;
-      cand<D, SMEM>(st, a, idx, xo_h, mi, moli);
-      float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-      for (int k = 0; k < D; k++) acc[k] = ofr[k * a.cap + pl];
-      force_tail<D>(s, sh.walls, a, gi, xo_h, mi, acc);
-    }
-    __syncthreads();
-  }
-}
-
-template <int D, int TPP = 4>
-__global__ void __launch_bounds__(BLOCK, RD_FORCE_MIN_BLOCKS) k_force(Args a) {
-  extern __shared__ __align__(16) uint32_t dyn[];
-  __shared__ TileShared<D> sh;
-  const Tile t = a.tiles[blockIdx.x];
-  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
-  if (sh.use_smem) force_tile<D, TPP, true>(sh, st, a, dyn);
-  else force_tile<D, TPP, false>(sh, st, a, dyn);
-}
-
 // ---------------------------------------------------------------------------
-// Reaction kernel.  Phase A: TPP threads per own particle count, for every
-// neighbour-dependent reaction, the listed partners of the right type within
-// r0 (16-bit counters, two reactions per word).  Phase B: one thread per own
-// particle forms the float64 propensities in file order, draws and writes the
-// new type (pyrdsim.pyx:2091-2222).
+// Propensity of one reaction for a particle of type ti with c counted
+// neighbours (pyrdsim.pyx:2091-2206).
 __device__ inline double rx_rate(const RxDev& R, int ti, int c) {
   double v = 0.0;  // reaction_rates[r, particle]
   if (R.reactant != ti) return v;
@@ -676,9 +400,10 @@ __device__ inline double rx_rate(const RxDev& R, int ti, int c) {
 // Per-particle tail of the reaction kernels, on one thread per particle:
 // float64 propensities in file order, the draw and the new type
 // (pyrdsim.pyx:2091-2222).  cw holds the neighbour counts of the
-// neighbour-dependent reactions, two 16-bit counters per word.
+// neighbour-dependent reactions, two 16-bit counters per word; pid is the
+// particle's caller index.
 __device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& a, int gi,
-                                  uint32_t mi, const uint32_t* cw) {
+                                  int pid, uint32_t mi, const uint32_t* cw) {
   const int ti = mi & 0xff;
   int newt = ti;
   const bool any = (s.rx_any_mask >> ti) & 1;
@@ -698,11 +423,10 @@ __device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& 
     }
   }
   if (a.flags & F_RATES_ONLY) {
-    a.rates_out[a.pid[gi]] = total;
+    a.rates_out[pid] = total;
     return;
   }
   if (any) {  // pyrdsim.pyx:2211-2222
-    const int pid = a.pid[gi];
     double u1;
     U4 w;
     if (a.flags & F_INJECT) {
@@ -726,181 +450,6 @@ __device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& 
     }
   }
   a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
-}
-
-template <int D, int TPP, bool SMEM>
-__device__ void react_tile(TileShared<D>& sh, const Staged<D>& st, const Args& a,
-                           uint32_t* dyn) {
-  const SysDev& s = sh.sys;
-  const TmplDev* tmpl = a.tmpl;
-  int* oidx = reinterpret_cast<int*>(dyn + 6 * a.cap);
-  uint32_t* ocnt = dyn + 7 * a.cap;  // [MAXR/2][cap]
-  const int tid = threadIdx.x;
-  const int groups = BLOCK / TPP, g = tid / TPP, lane_g = tid % TPP;
-  const int nhc = sh.nhc, nown = sh.nown;
-  float unit[3];
-#pragma unroll
-  for (int k = 0; k < D; k++) unit[k] = s.unit_hi[k];
-  const float Rrx2 = s.Rrx2;
-  for (int base = 0; base < nown; base += a.cap) {
-    const int nch = min(a.cap, nown - base);
-    for (int p0 = 0; p0 < nch; p0 += groups) {
-      const int pl = p0 + g;
-      const bool active = pl < nch;
-      uint32_t c0 = 0u, c1 = 0u, c2 = 0u, c3 = 0u;  // two 16-bit counters each
-      int idx = 0;
-      if (active) {
-        int q;
-        idx = own_index<SMEM>(sh.pc, nhc, base + pl, &q);
-        uint32_t xi_h[3] = {0u, 0u, 0u}, mi;
-        int moli;
-        cand<D, SMEM>(st, a, idx, xi_h, mi, moli);
-        const int ti = mi & 0xff;
-        if ((s.rx_nb_mask >> ti) & 1) {
-          const int gi = cand_gi<D, SMEM>(st, idx);
-          const int trbi = (mi >> 8) & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
-          const unsigned int pmask = s.partner[trbi];
-          const uint32_t bmask = tmi != 0xff ? tmpl[tmi].bondmask[loci] : 0u;
-          for_candidates<D, TPP, SMEM>(sh, q, lane_g, [&](int j) {
-            if (j == idx) return;
-            uint32_t xj[3] = {0u, 0u, 0u}, mj;
-            int molj;
-            cand<D, SMEM>(st, a, j, xj, mj, molj);
-            float r2 = 0.f;
-#pragma unroll
-            for (int k = 0; k < D; k++) {
-              const float dx = (float)(int)(xj[k] - xi_h[k]) * unit[k];
-              r2 += dx * dx;
-            }
-            if (!(r2 < Rrx2)) return;
-            bool listed;
-            if (molj == moli) listed = (bmask >> ((mj >> 16) & 31)) & 1;
-            else listed = (pmask >> ((mj >> 8) & 0xff)) & 1;
-            if (!listed) return;
-            const unsigned int rm = s.rxmatch[ti * MAXT + (mj & 0xff)];
-            double dexact = -1.0;
-            for (unsigned int mm = rm; mm; mm &= mm - 1u) {
-              const int r = __ffs(mm) - 1;
-              const RxDev& R = sh.rx[r];
-              bool inside;
-              if (r2 < R.r02_lo) inside = true;
-              else if (r2 > R.r02_hi) inside = false;
-              else {
-                if (dexact < 0) dexact = exact_dist<D>(s, a, gi, cand_gi<D, SMEM>(st, j));
-                inside = dexact < R.r0;
-              }
-              if (inside) {
-                const uint32_t inc = 1u << (16 * (r & 1));
-                switch (r >> 1) {
-                  case 0: c0 += inc; break;
-                  case 1: c1 += inc; break;
-                  case 2: c2 += inc; break;
-                  default: c3 += inc; break;
-                }
-              }
-            }
-          });
-        }
-      }
-#pragma unroll
-      for (int o = TPP >> 1; o > 0; o >>= 1) {
-        c0 += __shfl_xor_sync(0xffffffffu, c0, o);
-        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
-        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
-        c3 += __shfl_xor_sync(0xffffffffu, c3, o);
-      }
-      if (active && lane_g == 0) {
-        oidx[pl] = idx;
-        ocnt[0 * a.cap + pl] = c0;
-        ocnt[1 * a.cap + pl] = c1;
-        ocnt[2 * a.cap + pl] = c2;
-        ocnt[3 * a.cap + pl] = c3;
-      }
-    }
-    __syncthreads();
-    for (int pl = tid; pl < nch; pl += BLOCK) {
-      const int idx = oidx[pl];
-      const int gi = cand_gi<D, SMEM>(st, idx);
-      uint32_t xo_h[3], mi;
-      int moli;
-      cand<D, SMEM>(st, a, idx, xo_h, mi, moli);
-      const uint32_t cw[4] = {ocnt[0 * a.cap + pl], ocnt[1 * a.cap + pl], ocnt[2 * a.cap + pl],
-                              ocnt[3 * a.cap + pl]};
-      react_tail(s, sh.rx, a, gi, mi, cw);
-    }
-    __syncthreads();
-  }
-}
-
-template <int D, int TPP = 4>
-__global__ void __launch_bounds__(BLOCK, RD_REACT_MIN_BLOCKS) k_react(Args a) {
-  extern __shared__ __align__(16) uint32_t dyn[];
-  __shared__ TileShared<D> sh;
-  const Tile t = a.tiles[blockIdx.x];
-  Staged<D> st = tile_setup<D>(sh, a, t, dyn);
-  if (sh.use_smem) react_tile<D, TPP, true>(sh, st, a, dyn);
-  else react_tile<D, TPP, false>(sh, st, a, dyn);
-}
-
-// Per-tile staging plan, once per rebuild (see PlanCell).
-template <int D>
-__global__ void __launch_bounds__(BLOCK) k_plan(const SysDev* sysv, const Tile* tiles,
-                                                const int* cell_start, PlanCell* plan,
-                                                PlanHead* head, int stride) {
-  __shared__ int v[2 * BLOCK], o[2 * BLOCK], warp_tmp[BLOCK / 32], tot[2];
-  const Tile t = tiles[blockIdx.x];
-  const SysDev& s = sysv[t.sys];
-  const int tid = threadIdx.x;
-  int gb[2] = {0, 0};
-  for (int r = 0; r < 2; r++) {
-    const int q = tid + r * BLOCK;
-    int c = 0, interior = 0;
-    if (q < t.nhc) {
-      bool inb = true;
-      interior = 1;
-      int rem = q, g = 0, mult = 1;
-      for (int k = 0; k < D; k++) {
-        const int hc = rem % t.hdim[k];
-        rem /= t.hdim[k];
-        if (hc < s.halo[k] || hc >= s.halo[k] + t.w[k]) interior = 0;
-        int ck = t.c[k] - s.halo[k] + hc;
-        if ((s.periodic >> k) & 1) {
-          if (ck < 0) ck += s.nc[k];
-          if (ck >= s.nc[k]) ck -= s.nc[k];
-        } else if (ck < 0 || ck >= s.nc[k]) {
-          inb = false;
-        }
-        g += ck * mult;
-        mult *= s.nc[k];
-      }
-      if (inb) {
-        gb[r] = cell_start[s.c0 + g];
-        c = cell_start[s.c0 + g + 1] - gb[r];
-      }
-    }
-    v[q] = c;
-    o[q] = interior ? c : 0;
-  }
-  __syncthreads();
-  scan_pairs(v, warp_tmp, &tot[0]);
-  scan_pairs(o, warp_tmp, &tot[1]);
-  for (int r = 0; r < 2; r++) {
-    const int q = tid + r * BLOCK;
-    if (q >= t.nhc) continue;
-    PlanCell pc;
-    pc.beg = v[q];
-    pc.cnt = (q + 1 < 2 * BLOCK ? v[q + 1] : tot[0]) - v[q];
-    pc.gbeg = gb[r];
-    pc.own = o[q];
-    plan[(size_t)blockIdx.x * stride + q] = pc;
-  }
-  if (tid == 0) {
-    PlanHead h;
-    h.total = tot[0];
-    h.nown = tot[1];
-    h.pad0 = h.pad1 = 0;
-    head[blockIdx.x] = h;
-  }
 }
 
 // ---------------------------------------------------------------------------

@@ -2,12 +2,12 @@
 //
 // At every rebuild k_nlist writes, for each particle in sorted order, the
 // particles of the 3^D cells around its cell that lie within the list radius
-// (range + 2 sqrt(D) delta) and form a listed pair at that rebuild:
+// (range + 2 delta) and form a listed pair at that rebuild:
 // interaction partners (types at the rebuild, pyrdsim.pyx:1448-1587) of
 // another molecule, or bonded-list members of its own molecule (flagged with
 // LIST_SAME_MOL: they count for reactions, not for pair forces).  The drift
 // kernel's displacement check bounds every particle's motion since the
-// rebuild by delta per dimension, so every pair that comes within range
+// rebuild by delta (Euclidean), so every pair that comes within range
 // during the rebuild period is in the list, and each step kernel applies the
 // same distance tests as the reference to the listed pairs only.
 //
@@ -39,7 +39,7 @@
 
 namespace rd {
 
-constexpr int LBLOCK = 128;                    // threads per CTA
+constexpr int LBLOCK = BLOCK;                  // threads per CTA
 constexpr int LIST_SAME_MOL = (int)0x80000000;
 constexpr int BUILD_LANES = 8;                 // lanes per particle in k_nlist
 
@@ -59,32 +59,47 @@ struct ListShared {
   RxDev rx[MAXR];
 };
 
-// The CTA's run of particles: from blockIdx for a single system, else from
-// the chunk table.
+// Run of particles number q (PER per run): computed for a single system,
+// else from the chunk table.
 template <int PER>
-__device__ inline Chunk chunk_of(const Args& a) {
+__device__ inline Chunk chunk_at(const Args& a, int q) {
   if (a.single) {
     Chunk c = a.chunk1;
-    c.beg = blockIdx.x * PER;
+    c.beg = q * PER;
     c.cnt = min(PER, a.n_total - c.beg);
     return c;
   }
-  return a.chunks[blockIdx.x];
+  return a.chunks[q];
 }
 
-__device__ inline void list_tables(ListShared& sh, const Args& a, const Chunk& c, bool laws,
-                                   bool walls, bool rx) {
-  copy_words(reinterpret_cast<int*>(&sh.sys), reinterpret_cast<const int*>(&a.sys[c.sys]),
-             (int)(sizeof(SysDev) / 4));
-  if (laws)
-    copy_words(reinterpret_cast<int*>(sh.laws), reinterpret_cast<const int*>(a.laws + c.law0),
-               c.nlaws * (int)(sizeof(PairLaw) / 4));
-  if (walls)
-    copy_words(reinterpret_cast<int*>(sh.walls), reinterpret_cast<const int*>(a.walls + c.wall0),
-               c.nwalls * (int)(sizeof(WallLaw) / 4));
-  if (rx)
-    copy_words(reinterpret_cast<int*>(sh.rx), reinterpret_cast<const int*>(a.rx + c.rx0),
-               c.nrx * (int)(sizeof(RxDev) / 4));
+template <int PER>
+__device__ inline Chunk chunk_of(const Args& a) {
+  return chunk_at<PER>(a, (int)blockIdx.x);
+}
+
+// The chunk's system tables into shared memory: one round trip (all loads
+// first, then the stores; the caller synchronises).
+template <bool LAWS, bool WALLS, bool RX>
+__device__ inline void list_tables(ListShared& sh, const Args& a, const Chunk& c) {
+  constexpr int NS = (int)(sizeof(SysDev) / 4);
+  constexpr int NL = LAWS ? MAXI * (int)(sizeof(PairLaw) / 4) : 0;
+  constexpr int NW = WALLS ? MAXW * (int)(sizeof(WallLaw) / 4) : 0;
+  constexpr int NR = RX ? MAXR * (int)(sizeof(RxDev) / 4) : 0;
+  const int nl = c.nlaws * (int)(sizeof(PairLaw) / 4);
+  const int nw = c.nwalls * (int)(sizeof(WallLaw) / 4);
+  const int nr = c.nrx * (int)(sizeof(RxDev) / 4);
+  WordLoad<NS> ls;
+  WordLoad<NL> ll;
+  WordLoad<NW> lw;
+  WordLoad<NR> lr;
+  ls.load(reinterpret_cast<const int*>(&a.sys[c.sys]), NS);
+  if (LAWS) ll.load(reinterpret_cast<const int*>(a.laws + c.law0), nl);
+  if (WALLS) lw.load(reinterpret_cast<const int*>(a.walls + c.wall0), nw);
+  if (RX) lr.load(reinterpret_cast<const int*>(a.rx + c.rx0), nr);
+  ls.store(reinterpret_cast<int*>(&sh.sys), NS);
+  if (LAWS) ll.store(reinterpret_cast<int*>(sh.laws), nl);
+  if (WALLS) lw.store(reinterpret_cast<int*>(sh.walls), nw);
+  if (RX) lr.store(reinterpret_cast<int*>(sh.rx), nr);
 }
 
 // Prefetch into L1 the list words of this warp's particles: column block q
@@ -102,16 +117,59 @@ __device__ inline void prefetch_rows(const Args& a, const Chunk& ch, int cnt, bo
   }
 }
 
+// Cells of one row of particle cell c (offsets dy, dz): the cell index of
+// x = 0 in that row and one or two runs of x cells [lo0, hi0], [lo1, hi1]
+// (hi1 < lo1: none), in dx order.  False if the row lies outside a
+// reflecting box.
+template <int D>
+__device__ inline bool row_runs(const SysDev& s, const int* c, int dy, int dz, int& row, int& lo0,
+                                int& hi0, int& lo1, int& hi1) {
+  const int nx = s.nc[0], cx = c[0];
+  row = 0;
+  if (D > 1) {
+    int mult = nx;
+#pragma unroll
+    for (int k = 1; k < D; k++) {
+      int ck = c[k] + (k == 1 ? dy : dz);
+      if ((s.periodic >> k) & 1) {
+        if (ck < 0) ck += s.nc[k];
+        else if (ck >= s.nc[k]) ck -= s.nc[k];
+      } else if (ck < 0 || ck >= s.nc[k]) {
+        return false;
+      }
+      row += ck * mult;
+      mult *= s.nc[k];
+    }
+  }
+  lo1 = 0;
+  hi1 = -1;
+  if (s.halo[0] == 0) {
+    lo0 = hi0 = cx;
+  } else if (s.periodic & 1) {  // nx >= 3 here
+    if (cx == 0) { lo0 = hi0 = nx - 1; lo1 = 0; hi1 = 1; }
+    else if (cx == nx - 1) { lo0 = nx - 2; hi0 = nx - 1; lo1 = hi1 = 0; }
+    else { lo0 = cx - 1; hi0 = cx + 1; }
+  } else {
+    lo0 = max(cx - 1, 0);
+    hi0 = min(cx + 1, nx - 1);
+  }
+  return true;
+}
+
 // The list row of sorted particle i, generated from the cells and the
 // positions at the last rebuild (xr).  Candidates are visited in a fixed
 // order (rows of cells in dz, dy order; along x the adjacent cells form one
-// or two contiguous runs of the sorted arrays, in dx order).  L lanes test L
-// candidates per round; hits are numbered in candidate order and hit e is
-// handed to lane e % L, which calls emit(e, entry).  Returns the number of
-// entries.  The entry order does not depend on L.  All lanes of the group
-// must call it together.
+// or two contiguous runs of the sorted arrays, in dx order).  All run
+// boundaries are loaded at once, then the L lanes enumerate the candidates
+// of all runs together, L per round, two rounds per batch of loads.  Hits are
+// numbered in candidate order and hit e is handed to lane e % L, which calls
+// emit(e, entry).  Returns the number of entries.  The entry order does not
+// depend on L.  All lanes of the group must call it together.
 template <int D, int L, class Emit>
 __device__ inline int row_scan(const SysDev& s, const Args& a, int i, int lane, Emit&& emit) {
+  constexpr int NROW = D == 3 ? 9 : (D == 2 ? 3 : 1);
+  constexpr int NRUN = 2 * NROW;
+  constexpr int U = 2;
   const unsigned int gshift = (threadIdx.x & 31) & ~(L - 1);
   const unsigned int gmask = (L == 32 ? 0xffffffffu : ((1u << L) - 1u)) << gshift;
   uint32_t xi[3] = {0u, 0u, 0u};
@@ -127,84 +185,88 @@ __device__ inline int row_scan(const SysDev& s, const Args& a, int i, int lane, 
   const unsigned int pmask = s.partner[trbi];
   const uint32_t bmask = tmi != 0xff ? a.tmpl[tmi].bondmask[loci] : 0u;
   const float Rl2 = s.Rl2;
-  const int nx = s.nc[0], cx = c[0];
   const int h1 = D > 1 ? s.halo[1] : 0;
   const int h2 = D > 2 ? s.halo[2] : 0;
+  // runs [rb, re) of the sorted arrays, in candidate order
+  int rb[NRUN], re[NRUN];
+#pragma unroll
+  for (int q = 0; q < NROW; q++) {
+    const int dz = D == 3 ? q / 3 - 1 : 0;
+    const int dy = D >= 2 ? q % 3 - 1 : 0;
+    int row, lo0, hi0, lo1, hi1;
+    const bool ok = dy >= -h1 && dy <= h1 && dz >= -h2 && dz <= h2 &&
+                    row_runs<D>(s, c, dy, dz, row, lo0, hi0, lo1, hi1);
+    const int* cs = a.cell_start + s.c0 + row;
+    rb[2 * q] = ok ? cs[lo0] : 0;
+    re[2 * q] = ok ? cs[hi0 + 1] : 0;
+    const bool two = ok && hi1 >= lo1;
+    rb[2 * q + 1] = two ? cs[lo1] : 0;
+    re[2 * q + 1] = two ? cs[hi1 + 1] : 0;
+  }
+  int total = 0;
+#pragma unroll
+  for (int q = 0; q < NRUN; q++) total += re[q] - rb[q];
   int cnt = 0;
-  for (int dz = -h2; dz <= h2; dz++)
-    for (int dy = -h1; dy <= h1; dy++) {
-      // cell index of (x = 0, this row)
-      int row = 0;
-      bool inside = true;
-      if (D > 1) {
-        int mult = nx;
+  for (int base = 0; base < total; base += U * L) {
+    int jj[U];
+    uint32_t xx[U][3], mj[U];
+    int molj[U];
 #pragma unroll
-        for (int k = 1; k < D; k++) {
-          int ck = c[k] + (k == 1 ? dy : dz);
-          if ((s.periodic >> k) & 1) {
-            if (ck < 0) ck += s.nc[k];
-            else if (ck >= s.nc[k]) ck -= s.nc[k];
-          } else if (ck < 0 || ck >= s.nc[k]) {
-            inside = false;
-          }
-          row += ck * mult;
-          mult *= s.nc[k];
-        }
-      }
-      if (!inside) continue;
-      // one or two runs of x cells [lo0, hi0], [lo1, hi1]
-      int lo0, hi0, lo1 = 0, hi1 = -1;
-      if (s.halo[0] == 0) {
-        lo0 = hi0 = cx;
-      } else if (s.periodic & 1) {  // nx >= 3 here
-        if (cx == 0) { lo0 = hi0 = nx - 1; lo1 = 0; hi1 = 1; }
-        else if (cx == nx - 1) { lo0 = nx - 2; hi0 = nx - 1; lo1 = hi1 = 0; }
-        else { lo0 = cx - 1; hi0 = cx + 1; }
-      } else {
-        lo0 = max(cx - 1, 0);
-        hi0 = min(cx + 1, nx - 1);
-      }
-      const int* cs = a.cell_start + s.c0 + row;
-      const int b0 = cs[lo0], e0 = cs[hi0 + 1];
-      const int b1 = hi1 >= lo1 ? cs[lo1] : 0, e1 = hi1 >= lo1 ? cs[hi1 + 1] : 0;
-      const int n0 = e0 - b0, ntot = n0 + (e1 - b1);
-      for (int base = 0; base < ntot; base += L) {
-        const int t = base + lane;
-        const int j = t < n0 ? b0 + t : b1 + (t - n0);
-        int ent = 0;
-        bool hit = false;
-        if (t < ntot && j != i) {
-          float r2 = 0.f;
+    for (int u = 0; u < U; u++) {
+      // candidate t -> sorted index
+      int off = base + u * L + lane, j = -1;
 #pragma unroll
-          for (int k = 0; k < D; k++) {
-            const float d = (float)(int)(a.xr[k][j] - xi[k]) * s.unit_hi[k];
-            r2 += d * d;
-          }
-          if (r2 < Rl2) {
-            const uint32_t mj = a.meta[j];
-            if (a.mol[j] == moli) {
-              hit = (bmask >> ((mj >> 16) & 31)) & 1;
-              ent = j | LIST_SAME_MOL;
-            } else {
-              hit = (pmask >> ((mj >> 8) & 0xff)) & 1;
-              ent = j;
-            }
-          }
+      for (int q = 0; q < NRUN; q++) {
+        const int len = re[q] - rb[q];
+        if (j < 0) {
+          if (off < len) j = rb[q] + off;
+          else off -= len;
         }
-        const unsigned int m = (__ballot_sync(gmask, hit) & gmask) >> gshift;
-        const int nh = __popc(m);
-        const int r = (lane - cnt) & (L - 1);  // this lane takes hit cnt + r
-        int src = lane;
-        if (r < nh) {
-          unsigned int mm = m;
-          for (int q = 0; q < r; q++) mm &= mm - 1u;
-          src = __ffs(mm) - 1;
-        }
-        const int v = __shfl_sync(gmask, ent, src, L);
-        if (r < nh) emit(cnt + r, v);
-        cnt += nh;
       }
+      jj[u] = j;
+      const int jl = j < 0 ? i : j;
+#pragma unroll
+      for (int k = 0; k < 3; k++) xx[u][k] = k < D ? a.xr[k][jl] : 0u;
+      mj[u] = a.meta[jl];
+      molj[u] = a.mol[jl];
     }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (base + u * L >= total) break;  // uniform across the group
+      const int j = jj[u];
+      int ent = 0;
+      bool hit = false;
+      if (j >= 0 && j != i) {
+        float r2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          const float d = (float)(int)(xx[u][k] - xi[k]) * s.unit_hi[k];
+          r2 += d * d;
+        }
+        if (r2 < Rl2) {
+          if (molj[u] == moli) {
+            hit = (bmask >> ((mj[u] >> 16) & 31)) & 1;
+            ent = j | LIST_SAME_MOL;
+          } else {
+            hit = (pmask >> ((mj[u] >> 8) & 0xff)) & 1;
+            ent = j;
+          }
+        }
+      }
+      const unsigned int m = (__ballot_sync(gmask, hit) & gmask) >> gshift;
+      const int nh = __popc(m);
+      const int r = (lane - cnt) & (L - 1);  // this lane takes hit cnt + r
+      int src = lane;
+      if (r < nh) {
+        unsigned int mm = m;
+        for (int q = 0; q < r; q++) mm &= mm - 1u;
+        src = __ffs(mm) - 1;
+      }
+      const int v = __shfl_sync(gmask, ent, src, L);
+      if (r < nh) emit(cnt + r, v);
+      cnt += nh;
+    }
+  }
   return cnt;
 }
 
@@ -255,15 +317,26 @@ __device__ inline void for_entries(const SysDev& s, const Args& a, int i, int la
 }
 
 // Rebuild: every particle's list row and entry count, BUILD_LANES lanes per
-// particle (the row order does not depend on the lane count).
+// particle (the row order does not depend on the lane count).  Each chunk of
+// the step kernels is split over 16 / TPP CTAs, one particle per group.
 template <int D, int TPP>
 __global__ void __launch_bounds__(LBLOCK) k_nlist(Args a) {
   constexpr int PER = LBLOCK / TPP;
   constexpr int L = BUILD_LANES;
+  constexpr int SUB = PER / (LBLOCK / L);
   __shared__ SysDev sys;
-  const Chunk ch = chunk_of<PER>(a);
-  copy_words(reinterpret_cast<int*>(&sys), reinterpret_cast<const int*>(&a.sys[ch.sys]),
-             (int)(sizeof(SysDev) / 4));
+  Chunk ch = chunk_at<PER>(a, (int)blockIdx.x / SUB);
+  {
+    const int sub0 = ((int)blockIdx.x % SUB) * (LBLOCK / L);
+    ch.beg += sub0;
+    ch.cnt = max(0, min(LBLOCK / L, ch.cnt - sub0));
+  }
+  {
+    constexpr int NS = (int)(sizeof(SysDev) / 4);
+    WordLoad<NS> ls;
+    ls.load(reinterpret_cast<const int*>(&a.sys[ch.sys]), NS);
+    ls.store(reinterpret_cast<int*>(&sys), NS);
+  }
   __syncthreads();
   const int g = threadIdx.x / L, lane = threadIdx.x % L;
   int* nbr = a.nbr_out;
@@ -275,6 +348,23 @@ __global__ void __launch_bounds__(LBLOCK) k_nlist(Args a) {
     });
     if (lane == 0) a.ncnt_out[i] = cnt;
   }
+}
+
+// Reaction prefilter for the next step (sorted particle gi of type ti): the
+// float64 total propensity of that step grows monotonically with every
+// neighbour count, so rxA + rxB * (list entries), with a relative margin far
+// above the rounding of the reference's repeated additions, bounds it from
+// above.  If dt times the bound does not exceed the next step's u1 (the same
+// counter-based draw the reaction kernel makes), the draw `dt * total > u1`
+// (pyrdsim.pyx:2211-2213) cannot succeed and the particle keeps its type.
+// Returns true when the draw may succeed (cnt: list entries, pid: caller
+// index).
+__device__ inline bool rx_may_react(const SysDev& s, const Args& a, int ti, int cnt, int pid) {
+  if (!((s.rx_any_mask >> ti) & 1)) return false;
+  const U4 w = noise_words(s.seed, eff_em_step(a), pid, 1u);
+  const double u1 = uniform53(w.x, w.y);
+  const double ub = fma(s.rxB[ti], (double)cnt, s.rxA[ti]) * (1.0 + 1e-6);
+  return __dmul_rn(s.dt, ub) > u1;
 }
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
@@ -301,13 +391,12 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   for (int k = 0; k < D; k++) xo[k] = a.xh[k][i];
   const uint32_t mi = a.meta[i];
   prefetch_rows<TPP>(a, ch, cnt, active);
-  list_tables(sh, a, ch, true, true, false);
+  list_tables<true, true, false>(sh, a, ch);
   __syncthreads();
   const SysDev& s = sh.sys;
   float acc[3] = {0.f, 0.f, 0.f};
   if (active && s.R2 > 0.f) {
     const int ti = mi & 0xff;
-    const float R2 = s.R2;
     for_entries<D, TPP>(s, a, i, lane, cnt, [&](const Nb& nb) {
       if (nb.v < 0) return;  // same molecule: reactions only
       float dx[3], r2 = 0.f;
@@ -316,9 +405,9 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
         dx[k] = (float)(int)(nb.x[k] - xo[k]) * s.unit_hi[k];
         r2 += dx[k] * dx[k];
       }
-      if (!(r2 < R2)) return;
-      const unsigned int pp = s.ppair[ti * MAXT + (nb.m & 0xff)];
-      if (!(pp & 31)) return;
+      const int tj = nb.m & 0xff;
+      if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
+      const unsigned int pp = s.ppair[ti * MAXT + tj];
       const float fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
 #pragma unroll
       for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
@@ -334,16 +423,39 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     for (int k = 0; k < D; k++) sacc[k][g] = acc[k];
   }
   __syncthreads();
+  const int ib = ch.beg + tid;
+  bool listed = false;
+  int4 rec = make_int4(0, 0, 0, 0);
   if (tid < ch.cnt) {
-    const int ib = ch.beg + tid;
     uint32_t xb[3] = {0u, 0u, 0u};
 #pragma unroll
     for (int k = 0; k < D; k++) xb[k] = a.xh[k][ib];
     float accb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < D; k++) accb[k] = sacc[k][tid];
-    force_tail<D>(s, sh.walls, a, ib, xb, a.meta[ib], accb);
+    const uint32_t mb = a.meta[ib];
+    force_tail<D>(s, sh.walls, a, ib, xb, mb, accb);
+    if (a.flags & F_RX_NEXT) {
+      a.meta_out[ib] = mb;  // the next step's types, unless its draw succeeds
+      rec = make_int4(ib, (int)mb, a.ncnt[ib], a.pid[ib]);
+      listed = rx_may_react(s, a, (int)(mb & 0xff), rec.z, rec.w);
+    }
   }
+  if (a.flags & F_RX_NEXT) {
+    // append the particles whose draw may succeed (warp-aggregated)
+    const unsigned int bal = __ballot_sync(0xffffffffu, listed);
+    if (bal) {
+      const int lane32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
+      const int p = (int)(eff_em_step(a) & 1);
+      int base = 0;
+      if (lane32 == leader) base = atomicAdd(a.rx_count + p, __popc(bal));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (listed) a.rx_list[(size_t)p * a.npad + base + __popc(bal & ((1u << lane32) - 1u))] = rec;
+    }
+  }
+  // the list of this step's parity was consumed by the reaction kernel that
+  // ran before this one: empty it for the next drift kernel
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[eff_step(a) & 1] = 0;
 }
 
 // Reaction kernel.  Phase A: TPP lanes per particle count, for every
@@ -367,7 +479,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
 #pragma unroll
   for (int k = 0; k < D; k++) xo[k] = a.xh[k][i];
   prefetch_rows<TPP>(a, ch, cnt, active);
-  list_tables(sh, a, ch, false, false, true);
+  list_tables<false, false, true>(sh, a, ch);
   __syncthreads();
   const SysDev& s = sh.sys;
   uint32_t c0 = 0u, c1 = 0u, c2 = 0u, c3 = 0u;
@@ -423,7 +535,89 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   if (tid < ch.cnt) {
     const int ib = ch.beg + tid;
     const uint32_t cw[4] = {scnt[0][tid], scnt[1][tid], scnt[2][tid], scnt[3][tid]};
-    react_tail(s, sh.rx, a, ib, a.meta[ib], cw);
+    react_tail(s, sh.rx, a, ib, a.pid[ib], a.meta[ib], cw);
+  }
+}
+
+// Reaction kernel of the steps the previous drift kernel prefiltered: that
+// kernel copied every type forward and listed the particles whose draw may
+// succeed; one warp per listed particle counts its neighbours over its list
+// (lanes over entries) and lane 0 forms the propensities and draws
+// (pyrdsim.pyx:2070-2223).  A single system's tables are staged in shared
+// memory; a batch's are read through L1.
+template <int D, int TPP>
+__global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
+  __shared__ SysDev sys1;
+  __shared__ RxDev rx1[MAXR];
+  const int p = (int)(eff_step(a) & 1);
+  const int n = a.rx_count[p];
+  if (a.single) {
+    constexpr int NS = (int)(sizeof(SysDev) / 4), NR = MAXR * (int)(sizeof(RxDev) / 4);
+    const int nr = a.chunk1.nrx * (int)(sizeof(RxDev) / 4);
+    WordLoad<NS> ls;
+    WordLoad<NR> lr;
+    ls.load(reinterpret_cast<const int*>(a.sys), NS);
+    lr.load(reinterpret_cast<const int*>(a.rx), nr);
+    ls.store(reinterpret_cast<int*>(&sys1), NS);
+    lr.store(reinterpret_cast<int*>(rx1), nr);
+  }
+  __syncthreads();
+  const int4* list = a.rx_list + (size_t)p * a.npad;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (int)(gridDim.x * LBLOCK / 32);
+  for (int q = (int)((blockIdx.x * LBLOCK + threadIdx.x) >> 5); q < n; q += nwarps) {
+    const int4 rec = list[q];
+    const int m = rec.x, cnt = rec.z, pid = rec.w;
+    const uint32_t mm = (uint32_t)rec.y;
+    const SysDev& s = a.single ? sys1 : a.sys[a.sid[m]];
+    const RxDev* rx = a.single ? rx1 : a.rx + s.rx0;
+    const int tm = mm & 0xff;
+    uint32_t cw[4] = {0u, 0u, 0u, 0u};
+    if ((s.rx_nb_mask >> tm) & 1) {
+      uint32_t xm[3] = {0u, 0u, 0u};
+#pragma unroll
+      for (int k = 0; k < D; k++) xm[k] = a.xh[k][m];
+      const float Rrx2 = s.Rrx2;
+      auto count = [&](int v, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t mj) {
+        const int j = v & 0x7fffffff;
+        const uint32_t xj[3] = {x0, x1, x2};
+        float r2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          const float d = (float)(int)(xj[k] - xm[k]) * s.unit_hi[k];
+          r2 += d * d;
+        }
+        if (!(r2 < Rrx2)) return;
+        const unsigned int rmask = s.rxmatch[tm * MAXT + (mj & 0xff)];
+        double dexact = -1.0;
+        for (unsigned int b = rmask; b; b &= b - 1u) {
+          const int r = __ffs(b) - 1;
+          const RxDev& R = rx[r];
+          bool inside;
+          if (r2 < R.r02_lo) inside = true;
+          else if (r2 > R.r02_hi) inside = false;
+          else {
+            if (dexact < 0) dexact = exact_dist<D>(s, a, m, j);
+            inside = dexact < R.r0;
+          }
+          if (inside) cw[r >> 1] += 1u << (16 * (r & 1));
+        }
+      };
+      if (cnt <= a.W) {
+        for (int e = lane; e < cnt; e += 32) {
+          const Nb nb = gather<D>(a, a.nbr[ell_index<TPP>(e, m, a.npad)]);
+          count(nb.v, nb.x[0], nb.x[1], nb.x[2], nb.m);
+        }
+      } else {
+        row_scan<D, 32>(s, a, m, lane, [&](int, int v) {
+          const Nb nb = gather<D>(a, v);
+          count(nb.v, nb.x[0], nb.x[1], nb.x[2], nb.m);
+        });
+      }
+#pragma unroll
+      for (int w = 0; w < 4; w++) cw[w] = __reduce_add_sync(0xffffffffu, cw[w]);
+    }
+    if (lane == 0) react_tail(s, rx, a, m, pid, mm, cw);
   }
 }
 

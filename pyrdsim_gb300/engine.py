@@ -86,8 +86,8 @@ class Engine:
     arrays at this interface are in the caller's order, systems concatenated.
     """
 
-    def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, tile_target=0,
-                 use_graphs=True, list_width=0):
+    def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, use_graphs=True,
+                 list_width=0, reaction_prefilter=None):
         self.lib = load_library()
         self.systems = list(systems)
         self.D = self.systems[0].model.N_dim
@@ -98,9 +98,10 @@ class Engine:
         opt.device = device
         opt.skin = skin
         opt.threads_per_particle = threads_per_particle
-        opt.tile_target = tile_target
         opt.use_graphs = 0 if use_graphs else -1
         opt.list_width = list_width
+        # None: automatic; True: whenever the rates allow; False: off
+        opt.reaction_prefilter = 0 if reaction_prefilter is None else (1 if reaction_prefilter else -1)
         h = C.c_void_p()
         _check(self.lib.rdsim_create(arr, len(self.systems), C.byref(opt), C.byref(h)))
         self.h = h

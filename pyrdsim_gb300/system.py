@@ -19,7 +19,7 @@ Differences, all deliberate:
   keeps pairs listed at earlier rebuilds);
 * GPU options are extra dictionary keys starting with ``gpu_``:
   ``gpu_device``, ``gpu_skin``, ``gpu_threads_per_particle``,
-  ``gpu_tile_target``.
+  ``gpu_list_width``.
 """
 from __future__ import annotations
 
@@ -179,7 +179,7 @@ class system:  # noqa: N801  (the reference's class name)
         eng = Engine([sd], device=int(self._gpu.get("device", 0)),
                      skin=float(self._gpu.get("skin", 0.0)),
                      threads_per_particle=int(self._gpu.get("threads_per_particle", 0)),
-                     tile_target=int(self._gpu.get("tile_target", 0)))
+                     list_width=int(self._gpu.get("list_width", 0)))
         self._engine = eng
         if verbose:
             print("Creating neighbor list and evaluating drift..done", end="\n")

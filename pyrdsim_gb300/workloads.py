@@ -60,12 +60,13 @@ def lj_fluid(n=1024, rho=0.5, seed=1, dt=1e-4):
     return model.SystemData(m, x, np.zeros(n, np.int32), mol, first)
 
 
-def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93"):
+def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93", k_on=0.1, k_off=1.0):
     """Two species: 0 inactive (WCA only), 1 active (LJ among actives, 9-3 wall).
 
-    Reactions: activation 0 -> 1 at rate 0.1; deactivation 1 -> 0 at rate 1.0
-    per active neighbour within 1.5 sigma.  ``wall="wall"`` swaps the 9-3 wall
-    for the reference's tanh wall (for running the same shape in the reference).
+    Reactions: activation 0 -> 1 at rate k_on (0.1); deactivation 1 -> 0 at
+    rate k_off (1.0) per active neighbour within 1.5 sigma.  ``wall="wall"``
+    swaps the 9-3 wall for the reference's tanh wall (for running the same
+    shape in the reference).
     """
     rng = np.random.default_rng(seed)
     L = np.sqrt(n / rho)
@@ -93,9 +94,9 @@ def active_wall_fluid(n=65536, rho=0.4, seed=2, dt=1e-4, wall="wall93"):
             w, w0,
         ],
         "reactions": [
-            {"type": "linear", "reactant": 0, "product": 1, "rate": 0.1},
+            {"type": "linear", "reactant": 0, "product": 1, "rate": k_on},
             {"type": "locally_catalyzed", "reactant": 1, "catalyst": 1, "product": 0,
-             "rate": 1.0, "r0": 1.5},
+             "rate": k_off, "r0": 1.5},
         ],
     }
     m = model.Model.from_dict(params)

@@ -188,7 +188,7 @@ def test_handles_with_different_staging_capacity():
     from pyrdsim_gb300 import workloads
     sds = workloads.ensemble(n_systems=6, n_min=256, n_max=4096)
     engines = [_engine([s], use_graphs=False) for s in sds]
-    caps = [e.info()["max_tile_particles"] for e in engines]
+    caps = [e.info()["list_width"] for e in engines]
     assert len(set(caps)) > 1, caps
     big = int(np.argmax(caps))
     # the largest-capacity handle, created before smaller ones, still steps
@@ -209,7 +209,7 @@ def test_list_overflow_rows_match(name):
     fx, sd = _case(name)
     full = _engine([sd], use_graphs=False)
     short = _engine([sd], use_graphs=False, list_width=8)
-    assert short.info()["max_tile_particles"] == 8
+    assert short.info()["list_width"] == 8
     np.testing.assert_array_equal(full.drift(), short.drift())
     np.testing.assert_array_equal(full.reaction_rates(), short.reaction_rates())
     for n in (7, 13):
@@ -231,3 +231,31 @@ def test_lanes_per_particle_variants(tpp):
     norm, per = drift_errors(eng.drift(), orc.drift())
     assert norm <= FORCE_RTOL and per <= FORCE_RTOL, (norm, per)
     np.testing.assert_array_equal(eng.reaction_rates(), orc.reaction_rates(recompute=True))
+
+
+@pytest.mark.parametrize("case", ["patchy", "active_wall_fluid"])
+def test_reaction_prefilter_is_exact(case):
+    """The drift kernel's bound on the next reaction draw only skips draws
+    that cannot succeed: with and without it the runs are bit-identical
+    (Philox noise, graph replays, call boundaries, rebuilds)."""
+    if case == "active_wall_fluid":
+        from pyrdsim_gb300 import workloads
+        sd = workloads.active_wall_fluid(n=2048, seed=5, k_on=20.0, k_off=50.0)
+    else:
+        sd = _case(case)[1]
+    on = _engine([sd], reaction_prefilter=True)
+    off = _engine([sd], reaction_prefilter=False)
+    assert on.info()["reaction_prefilter"] == 1, on.info()
+    assert off.info()["reaction_prefilter"] == 0
+    prev = on.state()[1]
+    changed = 0
+    for n in (5, 33, 64, 1, 97):
+        on.step(n)
+        off.step(n)
+        xa, ta = on.state()
+        xb, tb = off.state()
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(xa, xb)
+        changed += int((ta != prev).sum())
+        prev = ta
+    assert changed >= 5, "too few reactions to test the prefilter"
