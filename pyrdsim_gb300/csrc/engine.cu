@@ -233,11 +233,30 @@ Args make_args(rdsim_handle* h) {
   return a;
 }
 
+// Kernel launch with programmatic stream serialization: the kernel may be
+// scheduled while the previous kernel of the stream still runs (its launch
+// and table staging overlap that kernel's tail); every kernel waits
+// (griddepcontrol.wait) before it reads what earlier work writes.
+template <class... P, class... A>
+void launch(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, static_cast<P>(args)...);
+}
+
 template <int D, int TPP>
 void launch_list(rdsim_handle* h, bool react, const Args& a) {
   const dim3 grid((unsigned)h->chunks_h.size());
-  if (react) k_react_l<D, TPP><<<grid, LBLOCK, 0, h->stream>>>(a);
-  else k_force_l<D, TPP><<<grid, LBLOCK, 0, h->stream>>>(a);
+  if (react) launch(k_react_l<D, TPP>, grid, LBLOCK, h->stream, a);
+  else launch(k_force_l<D, TPP>, grid, LBLOCK, h->stream, a);
 }
 
 template <int D>
@@ -250,19 +269,19 @@ void launch_list_d(rdsim_handle* h, bool react, const Args& a) {
 
 template <int D>
 void launch_listed(rdsim_handle* h, unsigned g, const Args& a) {
-  if (h->ltpp == 1) k_react_listed<D, 1><<<g, LBLOCK, 0, h->stream>>>(a);
-  else if (h->ltpp == 2) k_react_listed<D, 2><<<g, LBLOCK, 0, h->stream>>>(a);
-  else if (h->ltpp == 8) k_react_listed<D, 8><<<g, LBLOCK, 0, h->stream>>>(a);
-  else k_react_listed<D, 4><<<g, LBLOCK, 0, h->stream>>>(a);
+  if (h->ltpp == 1) launch(k_react_listed<D, 1>, g, LBLOCK, h->stream, a);
+  else if (h->ltpp == 2) launch(k_react_listed<D, 2>, g, LBLOCK, h->stream, a);
+  else if (h->ltpp == 8) launch(k_react_listed<D, 8>, g, LBLOCK, h->stream, a);
+  else launch(k_react_listed<D, 4>, g, LBLOCK, h->stream, a);
 }
 
 template <int D>
 void launch_nlist(rdsim_handle* h, const Args& a) {
   const dim3 grid((unsigned)(h->chunks_h.size() * (BUILD_LANES / h->ltpp)));
-  if (h->ltpp == 1) k_nlist<D, 1><<<grid, LBLOCK, 0, h->stream>>>(a);
-  else if (h->ltpp == 2) k_nlist<D, 2><<<grid, LBLOCK, 0, h->stream>>>(a);
-  else if (h->ltpp == 8) k_nlist<D, 8><<<grid, LBLOCK, 0, h->stream>>>(a);
-  else k_nlist<D, 4><<<grid, LBLOCK, 0, h->stream>>>(a);
+  if (h->ltpp == 1) launch(k_nlist<D, 1>, grid, LBLOCK, h->stream, a);
+  else if (h->ltpp == 2) launch(k_nlist<D, 2>, grid, LBLOCK, h->stream, a);
+  else if (h->ltpp == 8) launch(k_nlist<D, 8>, grid, LBLOCK, h->stream, a);
+  else launch(k_nlist<D, 4>, grid, LBLOCK, h->stream, a);
 }
 
 void launch_step_kernel(rdsim_handle* h, bool react, const Args& a) {
@@ -276,26 +295,26 @@ unsigned nblk(int n, int b = 256) { return (unsigned)((n + b - 1) / b); }
 int rebuild(rdsim_handle* h) {
   const int n = h->N;
   ProfScope ps(h, P_REBUILD, 6);
-  CK(cudaMemsetAsync(h->cell_count, 0, sizeof(int) * (size_t)h->ncells, h->stream));
   uint32_t* const* x = h->xh[h->cx];
   if (h->D == 2)
-    k_bin<2><<<nblk(n), 256, 0, h->stream>>>(h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+    launch(k_bin<2>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
   else if (h->D == 3)
-    k_bin<3><<<nblk(n), 256, 0, h->stream>>>(h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+    launch(k_bin<3>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
   else
-    k_bin<1><<<nblk(n), 256, 0, h->stream>>>(h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
-  k_scan_partial<<<h->nscan, 256, 0, h->stream>>>(h->cell_count, h->ncells, h->bsum);
-  k_scan_final<<<h->nscan, 256, 0, h->stream>>>(h->cell_count, h->ncells, h->bsum, h->cell_start);
-  k_scatter<<<nblk(n), 256, 0, h->stream>>>(h->cell_of, h->rank_of, h->cell_start, n, h->tmp);
+    launch(k_bin<1>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+  launch(k_scan_partial, h->nscan, 256, h->stream, h->cell_count, h->ncells, h->bsum);
+  launch(k_scan_final, h->nscan, 256, h->stream, h->cell_count, h->ncells, h->bsum, h->cell_start);
+  launch(k_scatter, nblk(n), 256, h->stream, h->cell_of, h->rank_of, h->cell_start, n, h->tmp,
+         h->cell_count, h->ncells);
   Args a = make_args(h);
   OrderOut o;
   o.mol = h->mol[1 - h->co];
   o.pid = h->pid[1 - h->co];
   for (int k = 0; k < 3; k++) o.xr[k] = h->xr[k];
   o.slot_of = h->slot_of;
-  if (h->D == 2) k_order<2><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
-  else if (h->D == 3) k_order<3><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
-  else k_order<1><<<nblk(n), 256, 0, h->stream>>>(a, o, h->tmp, h->cell_of, h->cell_start, n);
+  if (h->D == 2) launch(k_order<2>, nblk(n), 256, h->stream, a, o, h->tmp, h->cell_of, h->cell_start, n);
+  else if (h->D == 3) launch(k_order<3>, nblk(n), 256, h->stream, a, o, h->tmp, h->cell_of, h->cell_start, n);
+  else launch(k_order<1>, nblk(n), 256, h->stream, a, o, h->tmp, h->cell_of, h->cell_start, n);
   h->cx = 1 - h->cx;
   h->cm = 1 - h->cm;
   h->co = 1 - h->co;
@@ -357,9 +376,9 @@ int em(rdsim_handle* h, long long step, int flags, const double* xi) {
   a.xi = xi;
   unsigned g = nblk(h->N);
   ProfScope ps(h, P_EM, 1);
-  if (h->D == 2) k_em<2><<<g, 256, 0, h->stream>>>(a, h->sid);
-  else if (h->D == 3) k_em<3><<<g, 256, 0, h->stream>>>(a, h->sid);
-  else k_em<1><<<g, 256, 0, h->stream>>>(a, h->sid);
+  if (h->D == 2) launch(k_em<2>, g, 256, h->stream, a, h->sid);
+  else if (h->D == 3) launch(k_em<3>, g, 256, h->stream, a, h->sid);
+  else launch(k_em<1>, g, 256, h->stream, a, h->sid);
   CK(cudaGetLastError());
   h->cx = 1 - h->cx;
   return 0;
@@ -368,9 +387,9 @@ int em(rdsim_handle* h, long long step, int flags, const double* xi) {
 int snapshot(rdsim_handle* h, double* fx, int* ft) {
   Args a = make_args(h);
   unsigned g = nblk(h->N);
-  if (h->D == 2) k_snapshot<2><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, fx, ft);
-  else if (h->D == 3) k_snapshot<3><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, fx, ft);
-  else k_snapshot<1><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, fx, ft);
+  if (h->D == 2) launch(k_snapshot<2>, g, 256, h->stream, h->sys_d, h->sid, a, fx, ft);
+  else if (h->D == 3) launch(k_snapshot<3>, g, 256, h->stream, h->sys_d, h->sid, a, fx, ft);
+  else launch(k_snapshot<1>, g, 256, h->stream, h->sys_d, h->sid, a, fx, ft);
   CK(cudaGetLastError());
   return 0;
 }
@@ -499,7 +518,7 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
       if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
       if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
     }
-    if (!rc) k_set_counter<<<1, 1, 0, h->stream>>>(h->step_dev, h->freq, 1);
+    if (!rc) launch(k_set_counter, 1, 1, h->stream, h->step_dev, h->freq, 1);
     cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
     if (rc) {
       if (g) cudaGraphDestroy(g);
@@ -519,7 +538,7 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
     h->cm = cm0;
     h->co = co0;
   }
-  if (h->step_dev_value != s) k_set_counter<<<1, 1, 0, h->stream>>>(h->step_dev, s, 0);
+  if (h->step_dev_value != s) launch(k_set_counter, 1, 1, h->stream, h->step_dev, s, 0);
   CK(cudaGetLastError());
   CK(cudaGraphLaunch(it->second.exec, h->stream));
   h->step_dev_value = s + h->freq;
@@ -1055,6 +1074,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->terms_d, terms.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->atomterm_d, atomterm.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_count, (size_t)h->ncells, &B))) return bail(rc);
+  // zero once; every rebuild leaves them zero for the next (k_scatter)
+  if (cudaMemsetAsync(h->cell_count, 0, sizeof(int) * (size_t)h->ncells, h->stream) != cudaSuccess)
+    return bail(fail(RDSIM_ERR_CUDA, "memset"));
   if ((rc = dalloc(&h->cell_start, (size_t)h->ncells + 1, &B))) return bail(rc);
   if ((rc = dalloc(&h->bsum, (size_t)h->nscan, &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_of, N, &B))) return bail(rc);

@@ -25,6 +25,15 @@ __device__ inline void record_error(ErrDev* e, int code, long long particle, int
   }
 }
 
+// Programmatic dependent launch: pdl_trigger lets the next kernel of the
+// stream be scheduled while this one runs; pdl_wait blocks until the kernels
+// before this one have completed and their writes are visible.  Every kernel
+// waits before it touches memory that earlier work writes; only tables
+// written at create time are read before the wait.  Without the launch
+// attribute both are no-ops.
+__device__ inline void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ inline void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ inline long long eff_step(const Args& a) {
   return a.step_base ? *a.step_base + a.step : a.step;
 }
@@ -33,6 +42,8 @@ __device__ inline long long eff_em_step(const Args& a) {
 }
 
 __global__ void k_set_counter(long long* c, long long v, int add) {
+  pdl_trigger();
+  pdl_wait();
   if (add) *c += v;
   else *c = v;
 }
@@ -456,6 +467,8 @@ __device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& 
 // Stand-alone EM update of every particle (first step of a call).
 template <int D>
 __global__ void k_em(Args a, const int* sid) {
+  pdl_trigger();
+  pdl_wait();
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= a.n_total) return;
   const SysDev& s = a.sys[sid[gi]];
@@ -470,6 +483,8 @@ __global__ void k_em(Args a, const int* sid) {
 template <int D>
 __global__ void k_bin(const SysDev* sysv, const int* sid, const uint32_t* x0, const uint32_t* x1,
                       const uint32_t* x2, int n, int* cell_of, int* rank_of, int* count) {
+  pdl_trigger();
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool valid = i < n;
@@ -501,6 +516,8 @@ constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = 256 * SCAN_ITEMS;
 
 __global__ void k_scan_partial(const int* count, int n, int* bsum) {
+  pdl_trigger();
+  pdl_wait();
   __shared__ int ws[8];
   const int base = blockIdx.x * SCAN_TILE;
   int s = 0;
@@ -519,6 +536,8 @@ __global__ void k_scan_partial(const int* count, int n, int* bsum) {
 }
 
 __global__ void k_scan_final(const int* count, int n, const int* bsum, int* start) {
+  pdl_trigger();
+  pdl_wait();
   __shared__ int ws[8];
   __shared__ int prefix;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -560,9 +579,13 @@ __global__ void k_scan_final(const int* count, int n, const int* bsum, int* star
   if (blockIdx.x == gridDim.x - 1 && tid == 255) start[n] = run;
 }
 
+// Also zeroes the cell counts (consumed by the scans) for the next rebuild.
 __global__ void k_scatter(const int* cell_of, const int* rank_of, const int* start, int n,
-                          int* tmp) {
+                          int* tmp, int* count, int ncells) {
+  pdl_trigger();
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int q = i; q < ncells; q += gridDim.x * blockDim.x) count[q] = 0;
   if (i >= n) return;
   tmp[start[cell_of[i]] + rank_of[i]] = i;
 }
@@ -579,6 +602,8 @@ struct OrderOut {
 template <int D>
 __global__ void k_order(Args a, OrderOut o, const int* tmp, const int* cell_of,
                         const int* start, int n) {
+  pdl_trigger();
+  pdl_wait();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int old = tmp[k];
@@ -609,6 +634,8 @@ __global__ void k_order(Args a, OrderOut o, const int* tmp, const int* cell_of,
 // Hooks (tests and reports).
 template <int D>
 __global__ void k_to_double(const SysDev* sysv, const int* sid, Args a, double* x, int* types) {
+  pdl_trigger();
+  pdl_wait();
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= a.n_total) return;
   const SysDev& s = sysv[sid[gi]];
@@ -621,6 +648,8 @@ __global__ void k_to_double(const SysDev* sysv, const int* sid, Args a, double* 
 // trajectory frame: positions (float64) and types in caller order
 template <int D>
 __global__ void k_snapshot(const SysDev* sysv, const int* sid, Args a, double* fx, int* ft) {
+  pdl_trigger();
+  pdl_wait();
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= a.n_total) return;
   const SysDev& s = sysv[sid[gi]];
@@ -634,6 +663,8 @@ __global__ void k_snapshot(const SysDev* sysv, const int* sid, Args a, double* f
 template <int D>
 __global__ void k_ref_cells(const SysDev* sysv, int sys, Args a, const double* cl, int p0, int n,
                             int pid0, int* out) {
+  pdl_trigger();
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const SysDev& s = sysv[sys];
@@ -652,6 +683,8 @@ template <int D>
 __global__ void k_pairs(const SysDev* sysv, int sys, Args a, const TmplDev* tmpl, double rs,
                         float rs2_hi, int p0, int n, int pid0, int* out, unsigned long long cap,
                         unsigned long long* count) {
+  pdl_trigger();
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const SysDev& s = sysv[sys];

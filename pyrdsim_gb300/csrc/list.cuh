@@ -325,6 +325,7 @@ __global__ void __launch_bounds__(LBLOCK) k_nlist(Args a) {
   constexpr int L = BUILD_LANES;
   constexpr int SUB = PER / (LBLOCK / L);
   __shared__ SysDev sys;
+  pdl_trigger();
   Chunk ch = chunk_at<PER>(a, (int)blockIdx.x / SUB);
   {
     const int sub0 = ((int)blockIdx.x % SUB) * (LBLOCK / L);
@@ -337,6 +338,7 @@ __global__ void __launch_bounds__(LBLOCK) k_nlist(Args a) {
     ls.load(reinterpret_cast<const int*>(&a.sys[ch.sys]), NS);
     ls.store(reinterpret_cast<int*>(&sys), NS);
   }
+  pdl_wait();
   __syncthreads();
   const int g = threadIdx.x / L, lane = threadIdx.x % L;
   int* nbr = a.nbr_out;
@@ -375,10 +377,13 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   constexpr int PER = LBLOCK / TPP;
   __shared__ ListShared sh;
   __shared__ float sacc[3][PER];
+  pdl_trigger();
   const Chunk ch = chunk_of<PER>(a);
   const int tid = threadIdx.x, g = tid / TPP, lane = tid % TPP;
   const bool active = g < ch.cnt;
   const int i = ch.beg + (active ? g : 0);
+  list_tables<true, true, false>(sh, a, ch);
+  pdl_wait();
   if (tid < ch.cnt) {  // phase B reads of particle beg + tid
     const int ib = ch.beg + tid;
     prefetch_l1(a.pid + ib);
@@ -391,7 +396,6 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   for (int k = 0; k < D; k++) xo[k] = a.xh[k][i];
   const uint32_t mi = a.meta[i];
   prefetch_rows<TPP>(a, ch, cnt, active);
-  list_tables<true, true, false>(sh, a, ch);
   __syncthreads();
   const SysDev& s = sh.sys;
   float acc[3] = {0.f, 0.f, 0.f};
@@ -468,7 +472,10 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   constexpr int PER = LBLOCK / TPP;
   __shared__ ListShared sh;
   __shared__ uint32_t scnt[4][PER];
+  pdl_trigger();
   const Chunk ch = chunk_of<PER>(a);
+  list_tables<false, false, true>(sh, a, ch);
+  pdl_wait();
   const int tid = threadIdx.x, g = tid / TPP, lane = tid % TPP;
   const bool active = g < ch.cnt;
   const int i = ch.beg + (active ? g : 0);
@@ -479,7 +486,6 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
 #pragma unroll
   for (int k = 0; k < D; k++) xo[k] = a.xh[k][i];
   prefetch_rows<TPP>(a, ch, cnt, active);
-  list_tables<false, false, true>(sh, a, ch);
   __syncthreads();
   const SysDev& s = sh.sys;
   uint32_t c0 = 0u, c1 = 0u, c2 = 0u, c3 = 0u;
@@ -549,8 +555,7 @@ template <int D, int TPP>
 __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
   __shared__ SysDev sys1;
   __shared__ RxDev rx1[MAXR];
-  const int p = (int)(eff_step(a) & 1);
-  const int n = a.rx_count[p];
+  pdl_trigger();
   if (a.single) {
     constexpr int NS = (int)(sizeof(SysDev) / 4), NR = MAXR * (int)(sizeof(RxDev) / 4);
     const int nr = a.chunk1.nrx * (int)(sizeof(RxDev) / 4);
@@ -561,6 +566,9 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
     ls.store(reinterpret_cast<int*>(&sys1), NS);
     lr.store(reinterpret_cast<int*>(rx1), nr);
   }
+  pdl_wait();
+  const int p = (int)(eff_step(a) & 1);
+  const int n = a.rx_count[p];
   __syncthreads();
   const int4* list = a.rx_list + (size_t)p * a.npad;
   const int lane = threadIdx.x & 31;
