@@ -142,9 +142,9 @@ class ClockSampler:
 
 
 def traffic_per_launch(n):
-    """dram bytes per k_force launch from the committed ncu summary (scaled by
-    particles if the capture was a smaller case), or None."""
-    path = os.path.join(ROOT, "profiles", "k_force_active_wall_fluid.md")
+    """dram bytes per k_force_l launch from the committed ncu summary (scaled
+    by particles if the capture was a smaller case), or None."""
+    path = os.path.join(ROOT, "profiles", "k_force_l_active_wall_fluid.md")
     try:
         with open(path) as f:
             for line in f:
@@ -302,7 +302,7 @@ def run_ours(args, rank, ws, local):
                 "path": "C ABI: rdsim_set_state (host) + rdsim_step + rdsim_get_state (host)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_force<2,4>",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_force_l<2,2>",
                      "algorithmic_bytes_per_launch": ALG_BYTES * N,
                      "avg_launch_us": f_ms * 1e3, "peak_source": peak_kind,
                      "react_avg_launch_us": r_ms * 1e3},

@@ -259,8 +259,9 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 /* Kernel accounting (no reference counterpart; measurement only).  Launch
  * counts are always kept; with profiling enabled every kernel launch is also
  * bracketed by CUDA events on the handle's stream and its device time summed
- * per class: 0 = drift (k_force), 1 = reactions (k_react), 2 = stand-alone
- * Euler-Maruyama (k_em), 3 = cell-list rebuild (5 kernels), 4 = hooks. */
+ * per class: 0 = drift (k_force_l), 1 = reactions (k_react_l,
+ * k_react_listed), 2 = stand-alone Euler-Maruyama (k_em), 3 = cell-list and
+ * Verlet-list rebuild (6 kernels), 4 = hooks. */
 #define RDSIM_PROFILE_CLASSES 5
 typedef struct {
   int64_t launches[RDSIM_PROFILE_CLASSES];
