@@ -49,7 +49,9 @@ struct WallLaw {
 
 // One reaction (pyrdsim.pyx:2070-2223).
 struct RxDev {
-  int kind, reactant, product, catalyst, inh, inh2, pad0, pad1;
+  int kind, reactant, product, catalyst, inh, inh2;
+  float ratef;                    // rate as float32, rounded up
+  int pad1;
   double rate, r0, dec;
   float r02_lo, r02_hi;           // guard band around r0^2
 };
@@ -101,6 +103,10 @@ struct SysDev {
   // rxA[t] + rxB[t] * (listed neighbours) >= the float64 total of a type-t
   // particle (linear and inhibited rates in rxA, catalysed rates in rxB).
   double rxA[MAXT], rxB[MAXT];
+  float rxAf[MAXT], rxBf[MAXT];   // the same as float32, rounded up
+  float dtf;                      // dt as float32, rounded up
+  int rx_screen_mask;             // types whose reactions are all linear or
+                                  // catalysed (float32 screening of draws)
 };
 
 // A run of consecutive particles (sorted order) of one system, handled by one

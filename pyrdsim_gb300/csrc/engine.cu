@@ -582,6 +582,13 @@ void free_all(rdsim_handle* h) {
 // 5e-7 r^2 (rounding of the unit, the conversion, the products and the sum)
 // plus 2 r sqrt(3) unit (truncation of both coordinates); the band is four
 // times wider.
+// The smallest float32 not below v (v >= 0).
+float float_up(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = std::nextafter(f, 3.0e38f);
+  return f;
+}
+
 float guard2(double r, double unit) {
   return (float)(r * r * 2e-6 + 2.0 * r * 4.0 * unit + 1e-12);
 }
@@ -650,6 +657,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     sd.n = S.n_particles;
     sd.ntypes = S.n_types;
     sd.dt = S.dt;
+    sd.dtf = float_up(S.dt);
     sd.seed = S.seed ^ (0x9E3779B97F4A7C15ULL * (unsigned long long)si);
     sd.angle_is_pi = S.angle_is_pi;
     hsys.p0 = h->N;
@@ -810,6 +818,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     if (sd.nlaws > MAXI) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many pair laws"));
     // reactions
     sd.rx0 = (int)rxs.size();
+    sd.rx_screen_mask = (1 << MAXT) - 1;
     float Rrx2 = 0.f;
     for (int q = 0; q < S.n_reactions; q++) {
       const rdsim_reaction& r = S.reactions[q];
@@ -824,6 +833,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       x.rate = r.rate;
       x.r0 = r.r0;
       x.dec = r.rate_decrease;
+      x.ratef = float_up(r.rate);
       if (r.product < 0 || r.product >= S.n_types || r.reactant < 0 || r.reactant >= MAXT)
         return bail(fail(RDSIM_ERR_UNSUPPORTED, "reaction types out of range"));
       if (r.kind != RDSIM_RX_LINEAR) {
@@ -850,12 +860,17 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       sd.rx_any_mask |= 1 << r.reactant;
       if (r.kind == RDSIM_RX_CATALYZED) sd.rxB[r.reactant] += r.rate;
       else sd.rxA[r.reactant] += r.rate;  // linear; inhibited at most its rate
+      if (r.kind == RDSIM_RX_INHIBITED) sd.rx_screen_mask &= ~(1 << r.reactant);
       if (!(r.rate >= 0.0 && std::isfinite(r.rate)) ||
           (r.kind == RDSIM_RX_INHIBITED && !(r.rate_decrease >= 0.0)))
         h->rx_pre = false;  // the bound needs non-negative rates
       rxs.push_back(x);
     }
     sd.nrx = S.n_reactions;
+    for (int t = 0; t < MAXT; t++) {  // bounds above the float64 sums
+      sd.rxAf[t] = float_up(sd.rxA[t] * (1.0 + 1e-12));
+      sd.rxBf[t] = float_up(sd.rxB[t] * (1.0 + 1e-12));
+    }
     if (S.n_reactions > 0) h->has_rx = true;
     sd.R2 = R2;
     sd.Rrx2 = Rrx2;

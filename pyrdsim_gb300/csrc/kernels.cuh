@@ -190,9 +190,41 @@ __device__ inline double uniform53(uint32_t hi, uint32_t lo) {
   return __dadd_rn(__dmul_rn(__ull2double_rn(m), 1.1102230246251565e-16), 5.551115123125783e-17);
 }
 
+// Counter-based draws of one particle at one step.  The tag-0 words give
+// the Gaussian increments (x, y; for D == 3 also z, w); the reaction
+// uniforms take u1 from tag-0 (z, w) for D <= 2 and from tag-1 (x, y) for
+// D == 3, and u2 from the other tag-1 pair.  w0 may hold the tag-0 words
+// of the step already.
 template <int D>
-__device__ inline void gaussians(unsigned long long seed, long long step, int pid, float* xi) {
-  U4 w = noise_words(seed, step, pid, 0u);
+__device__ inline void u1_words(unsigned long long seed, long long step, int pid, const U4* w0,
+                                uint32_t& hi, uint32_t& lo) {
+  if (D <= 2) {
+    const U4 w = w0 ? *w0 : noise_words(seed, step, pid, 0u);
+    hi = w.z;
+    lo = w.w;
+  } else {
+    const U4 w = noise_words(seed, step, pid, 1u);
+    hi = w.x;
+    lo = w.y;
+  }
+}
+
+template <int D>
+__device__ inline void u2_words(unsigned long long seed, long long step, int pid, uint32_t& hi,
+                                uint32_t& lo) {
+  const U4 w = noise_words(seed, step, pid, 1u);
+  hi = D <= 2 ? w.x : w.z;
+  lo = D <= 2 ? w.y : w.w;
+}
+
+// Float32 bounds [lo, hi] of uniform53(w_hi, w_lo): its top 24 bits.
+__device__ inline void uniform_bounds(uint32_t whi, float& lo, float& hi) {
+  lo = (float)(whi >> 8) * 5.9604644775390625e-08f;
+  hi = (float)((whi >> 8) + 1u) * 5.9604644775390625e-08f;
+}
+
+template <int D>
+__device__ inline void gaussians(const U4& w, float* xi) {
   float ua = (float)w.x * 2.3283064365386963e-10f + 1.1641532182693481e-10f;
   float r = sqrtf(-2.0f * logf(ua));
   float sn, cs;
@@ -212,14 +244,15 @@ __device__ inline void gaussians(unsigned long long seed, long long step, int pi
 // (pyrdsim.pyx:2240-2292): x += dt D a + sqrt(2 dt D) xi, then reflect or wrap.
 template <int D>
 __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid, int type,
-                                 const float* acc, long long em_step, int flags) {
+                                 const float* acc, long long em_step, int flags,
+                                 const U4* w0 = nullptr) {
   float xi[3] = {0.f, 0.f, 0.f};
   if (!(flags & F_NO_NOISE)) {
     if (flags & F_INJECT) {
 #pragma unroll
       for (int k = 0; k < D; k++) xi[k] = (float)a.xi[(size_t)pid * D + k];
     } else {
-      gaussians<D>(s.seed, em_step, pid, xi);
+      gaussians<D>(w0 ? *w0 : noise_words(s.seed, em_step, pid, 0u), xi);
     }
   }
   const float fp = s.fp[type], np = s.npf[type];
@@ -336,9 +369,9 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
 // checks, and the fused Euler-Maruyama update.  acc holds the pair drift.
 template <int D>
 __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const Args& a, int gi,
-                                  const uint32_t* xo_h, uint32_t mi, float* acc) {
+                                  int pid, const uint32_t* xo_h, uint32_t mi, float* acc,
+                                  const U4* w0 = nullptr) {
   const int ti = mi & 0xff;
-  const int pid = a.pid[gi];
   // walls (pyrdsim.pyx:1979-1986)
   for (int w = 0; w < s.nwalls; w++) {
     const WallLaw& W = walls[w];
@@ -389,7 +422,7 @@ __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const A
     if (rel2 > s.delta * s.delta)
       record_error(a.err, RDSIM_ERR_SKIN, pid, -1, (double)sqrtf(rel2), eff_step(a));
   }
-  if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags);
+  if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags, w0);
 }
 
 // ---------------------------------------------------------------------------
@@ -408,56 +441,121 @@ __device__ inline double rx_rate(const RxDev& R, int ti, int c) {
   return v < 0 ? 0.0 : v;
 }
 
+// Float64 total propensity of a type-ti particle (pyrdsim.pyx:2091-2206,
+// file order, repeated additions).
+__device__ inline double rx_total(const SysDev& s, const RxDev* rx, int ti, const uint32_t* cw) {
+  double total = 0.0;
+  for (int r = 0; r < s.nrx; r++) {
+    const RxDev& R = rx[r];
+    if (R.reactant != ti) continue;
+    const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
+    if (R.kind == RDSIM_RX_LINEAR) {
+      total = __dadd_rn(total, R.rate);
+    } else if (R.kind == RDSIM_RX_CATALYZED) {
+      for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
+    } else {
+      total = __dadd_rn(total, rx_rate(R, ti, c));
+    }
+  }
+  return total;
+}
+
 // Per-particle tail of the reaction kernels, on one thread per particle:
-// float64 propensities in file order, the draw and the new type
+// propensities in file order, the draw and the new type
 // (pyrdsim.pyx:2091-2222).  cw holds the neighbour counts of the
 // neighbour-dependent reactions, two 16-bit counters per word; pid is the
-// particle's caller index.
+// particle's caller index.  The reference decides in float64; when every
+// reaction of the type adds a non-negative term (linear, catalysed), the
+// two comparisons are first made in float32 against the bounds of the
+// uniforms with a relative margin of 4e-6 (the float32 sums err by less than
+// 1e-6), and only an undecided comparison is redone in float64.
+template <int D>
 __device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& a, int gi,
                                   int pid, uint32_t mi, const uint32_t* cw) {
   const int ti = mi & 0xff;
   int newt = ti;
   const bool any = (s.rx_any_mask >> ti) & 1;
-  double total = 0.0;
-  if (any) {
-    for (int r = 0; r < s.nrx; r++) {  // pyrdsim.pyx:2091-2206, file order
-      const RxDev& R = rx[r];
-      if (R.reactant != ti) continue;
-      const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
-      if (R.kind == RDSIM_RX_LINEAR) {
-        total = __dadd_rn(total, R.rate);
-      } else if (R.kind == RDSIM_RX_CATALYZED) {
-        for (int e = 0; e < c; e++) total = __dadd_rn(total, R.rate);
-      } else {
-        total = __dadd_rn(total, rx_rate(R, ti, c));
-      }
-    }
-  }
   if (a.flags & F_RATES_ONLY) {
-    a.rates_out[pid] = total;
+    a.rates_out[pid] = any ? rx_total(s, rx, ti, cw) : 0.0;
     return;
   }
   if (any) {  // pyrdsim.pyx:2211-2222
-    double u1;
-    U4 w;
-    if (a.flags & F_INJECT) {
-      u1 = a.u1[pid];
+    const long long step = eff_step(a);
+    const bool inject = (a.flags & F_INJECT) != 0;
+    // the uniforms and their float32 bounds
+    uint32_t h1 = 0, l1 = 0;
+    float u1lo, u1hi;
+    if (inject) {
+      u1lo = __double2float_rd(a.u1[pid]);
+      u1hi = __double2float_ru(a.u1[pid]);
     } else {
-      w = noise_words(s.seed, eff_step(a), pid, 1u);
-      u1 = uniform53(w.x, w.y);
+      u1_words<D>(s.seed, step, pid, nullptr, h1, l1);
+      uniform_bounds(h1, u1lo, u1hi);
     }
-    if (__dmul_rn(s.dt, total) > u1) {
-      const double u2 = (a.flags & F_INJECT) ? a.u2[pid] : uniform53(w.z, w.w);
-      double accu = 0.0;
+    const bool screen = (s.rx_screen_mask >> ti) & 1;
+    float tf = 0.f;
+    int fires = -1;  // -1: undecided
+    constexpr float M = 4e-6f;
+    if (screen) {
       for (int r = 0; r < s.nrx; r++) {
         const RxDev& R = rx[r];
+        if (R.reactant != ti) continue;
         const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
-        accu = __dadd_rn(accu, __ddiv_rn(rx_rate(R, ti, c), total));
-        if (accu >= u2) {
-          newt = R.product;
-          break;
+        tf += R.kind == RDSIM_RX_LINEAR ? R.ratef : R.ratef * (float)c;
+      }
+      const float p = s.dtf * tf;
+      if (p * (1.0f + M) < u1lo) fires = 0;
+      else if (p * (1.0f - M) > u1hi) fires = 1;
+    }
+    double total = -1.0;
+    if (fires < 0) {
+      total = rx_total(s, rx, ti, cw);
+      const double u1 = inject ? a.u1[pid] : uniform53(h1, l1);
+      fires = __dmul_rn(s.dt, total) > u1 ? 1 : 0;
+    }
+    if (fires) {
+      uint32_t h2 = 0, l2 = 0;
+      float u2lo, u2hi;
+      if (inject) {
+        u2lo = __double2float_rd(a.u2[pid]);
+        u2hi = __double2float_ru(a.u2[pid]);
+      } else {
+        u2_words<D>(s.seed, step, pid, h2, l2);
+        uniform_bounds(h2, u2lo, u2hi);
+      }
+      int pick = -1;  // reaction index; -1 undecided, nrx: none
+      if (screen && tf > 0.f) {
+        float acc = 0.f;
+        for (int r = 0; r < s.nrx && pick < 0; r++) {
+          const RxDev& R = rx[r];
+          float rf = 0.f;
+          if (R.reactant == ti) {
+            const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
+            rf = R.kind == RDSIM_RX_LINEAR ? R.ratef : R.ratef * (float)c;
+          }
+          acc += rf / tf;
+          if (acc * (1.0f + M) < u2lo) continue;  // not reached yet
+          if (acc * (1.0f - M) >= u2hi) pick = r;
+          else break;  // undecided
+        }
+        if (pick < 0 && acc * (1.0f + M) < u2lo) pick = s.nrx;  // no product reached
+      }
+      if (pick < 0) {  // exact selection (pyrdsim.pyx:2216-2222)
+        if (total < 0.0) total = rx_total(s, rx, ti, cw);
+        const double u2 = inject ? a.u2[pid] : uniform53(h2, l2);
+        double accu = 0.0;
+        pick = s.nrx;
+        for (int r = 0; r < s.nrx; r++) {
+          const RxDev& R = rx[r];
+          const int c = (cw[r >> 1] >> (16 * (r & 1))) & 0xffff;
+          accu = __dadd_rn(accu, __ddiv_rn(rx_rate(R, ti, c), total));
+          if (accu >= u2) {
+            pick = r;
+            break;
+          }
         }
       }
+      if (pick < s.nrx) newt = rx[pick].product;
     }
   }
   a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;

@@ -359,14 +359,21 @@ __global__ void __launch_bounds__(LBLOCK) k_nlist(Args a) {
 // above.  If dt times the bound does not exceed the next step's u1 (the same
 // counter-based draw the reaction kernel makes), the draw `dt * total > u1`
 // (pyrdsim.pyx:2211-2213) cannot succeed and the particle keeps its type.
-// Returns true when the draw may succeed (cnt: list entries, pid: caller
-// index).
-__device__ inline bool rx_may_react(const SysDev& s, const Args& a, int ti, int cnt, int pid) {
+// The bound and the comparison are float32: rxAf, rxBf and dtf are rounded
+// up, the relative margin 1e-5 covers the float32 rounding, and the uniform
+// is replaced by the lower bound of its top 24 bits.  Returns true when the
+// draw may succeed (cnt: list entries, pid: caller index, w0: the tag-0
+// words of the next step).
+template <int D>
+__device__ inline bool rx_may_react(const SysDev& s, const Args& a, int ti, int cnt, int pid,
+                                    const U4& w0) {
   if (!((s.rx_any_mask >> ti) & 1)) return false;
-  const U4 w = noise_words(s.seed, eff_em_step(a), pid, 1u);
-  const double u1 = uniform53(w.x, w.y);
-  const double ub = fma(s.rxB[ti], (double)cnt, s.rxA[ti]) * (1.0 + 1e-6);
-  return __dmul_rn(s.dt, ub) > u1;
+  uint32_t hi, lo;
+  u1_words<D>(s.seed, eff_em_step(a), pid, &w0, hi, lo);
+  float u1lo, u1hi;
+  uniform_bounds(hi, u1lo, u1hi);
+  const float ub = (s.rxAf[ti] + s.rxBf[ti] * (float)cnt) * (1.0f + 1e-5f);
+  return s.dtf * ub > u1lo;
 }
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
@@ -438,11 +445,17 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
 #pragma unroll
     for (int k = 0; k < D; k++) accb[k] = sacc[k][tid];
     const uint32_t mb = a.meta[ib];
-    force_tail<D>(s, sh.walls, a, ib, xb, mb, accb);
+    const int pid = a.pid[ib];
+    // one Philox call for the next step's noise and reaction uniform
+    const bool words = (a.flags & F_RX_NEXT) ||
+                       ((a.flags & F_EM) && !(a.flags & (F_NO_NOISE | F_INJECT)));
+    U4 w0 = {0u, 0u, 0u, 0u};
+    if (words) w0 = noise_words(s.seed, eff_em_step(a), pid, 0u);
+    force_tail<D>(s, sh.walls, a, ib, pid, xb, mb, accb, words ? &w0 : nullptr);
     if (a.flags & F_RX_NEXT) {
       a.meta_out[ib] = mb;  // the next step's types, unless its draw succeeds
-      rec = make_int4(ib, (int)mb, a.ncnt[ib], a.pid[ib]);
-      listed = rx_may_react(s, a, (int)(mb & 0xff), rec.z, rec.w);
+      rec = make_int4(ib, (int)mb, a.ncnt[ib], pid);
+      listed = rx_may_react<D>(s, a, (int)(mb & 0xff), rec.z, pid, w0);
     }
   }
   if (a.flags & F_RX_NEXT) {
@@ -541,7 +554,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   if (tid < ch.cnt) {
     const int ib = ch.beg + tid;
     const uint32_t cw[4] = {scnt[0][tid], scnt[1][tid], scnt[2][tid], scnt[3][tid]};
-    react_tail(s, sh.rx, a, ib, a.pid[ib], a.meta[ib], cw);
+    react_tail<D>(s, sh.rx, a, ib, a.pid[ib], a.meta[ib], cw);
   }
 }
 
@@ -625,7 +638,7 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
 #pragma unroll
       for (int w = 0; w < 4; w++) cw[w] = __reduce_add_sync(0xffffffffu, cw[w]);
     }
-    if (lane == 0) react_tail(s, rx, a, m, pid, mm, cw);
+    if (lane == 0) react_tail<D>(s, rx, a, m, pid, mm, cw);
   }
 }
 
