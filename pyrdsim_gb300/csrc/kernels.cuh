@@ -149,24 +149,24 @@ __device__ inline float pair_force(const SysDev& s, const PairLaw* laws, const A
 }
 
 // Block-wide copies of words from global to shared memory (blockDim.x ==
-// BLOCK).  All loads are issued before any store: through generic pointers
+// NT).  All loads are issued before any store: through generic pointers
 // the compiler could not otherwise move a load past the previous iteration's
 // store, and every iteration would wait a full memory round trip.
-template <int MAXN>
+template <int MAXN, int NT = BLOCK>
 struct WordLoad {
-  static constexpr int IT = MAXN > 0 ? (MAXN + BLOCK - 1) / BLOCK : 1;
+  static constexpr int IT = MAXN > 0 ? (MAXN + NT - 1) / NT : 1;
   int v[IT];
   __device__ inline void load(const int* __restrict__ src, int n) {
 #pragma unroll
     for (int u = 0; u < IT; u++) {
-      const int q = (int)threadIdx.x + u * BLOCK;
+      const int q = (int)threadIdx.x + u * NT;
       v[u] = q < n ? __ldg(src + q) : 0;
     }
   }
   __device__ inline void store(int* __restrict__ dst, int n) const {
 #pragma unroll
     for (int u = 0; u < IT; u++) {
-      const int q = (int)threadIdx.x + u * BLOCK;
+      const int q = (int)threadIdx.x + u * NT;
       if (q < n) dst[q] = v[u];
     }
   }

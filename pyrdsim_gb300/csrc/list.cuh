@@ -41,7 +41,6 @@ namespace rd {
 
 constexpr int LBLOCK = BLOCK;                  // threads per CTA
 constexpr int LIST_SAME_MOL = (int)0x80000000;
-constexpr int BUILD_LANES = 8;                 // lanes per particle in k_nlist
 
 template <int TPP>
 __device__ inline int ell_index(int e, int i, int npad) {
@@ -316,40 +315,120 @@ __device__ inline void for_entries(const SysDev& s, const Args& a, int i, int la
   }
 }
 
-// Rebuild: every particle's list row and entry count, BUILD_LANES lanes per
-// particle (the row order does not depend on the lane count).  Each chunk of
-// the step kernels is split over 16 / TPP CTAs, one particle per group.
+// Rebuild: every particle's list row and entry count, one thread per
+// particle and one CTA per run of LBLOCK / TPP particles.  The thread walks
+// the runs of its cell neighbourhood in candidate order (the order row_scan
+// uses), four candidates per batch of loads, and appends the listed pairs
+// within the list radius.
 template <int D, int TPP>
-__global__ void __launch_bounds__(LBLOCK) k_nlist(Args a) {
+__global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
   constexpr int PER = LBLOCK / TPP;
-  constexpr int L = BUILD_LANES;
-  constexpr int SUB = PER / (LBLOCK / L);
+  constexpr int NROW = D == 3 ? 9 : (D == 2 ? 3 : 1);
+  constexpr int NRUN = 2 * NROW;
+  constexpr int U = 4;
   __shared__ SysDev sys;
   pdl_trigger();
-  Chunk ch = chunk_at<PER>(a, (int)blockIdx.x / SUB);
-  {
-    const int sub0 = ((int)blockIdx.x % SUB) * (LBLOCK / L);
-    ch.beg += sub0;
-    ch.cnt = max(0, min(LBLOCK / L, ch.cnt - sub0));
-  }
+  const Chunk ch = chunk_at<PER>(a, (int)blockIdx.x);
   {
     constexpr int NS = (int)(sizeof(SysDev) / 4);
-    WordLoad<NS> ls;
+    WordLoad<NS, PER> ls;
     ls.load(reinterpret_cast<const int*>(&a.sys[ch.sys]), NS);
     ls.store(reinterpret_cast<int*>(&sys), NS);
   }
   pdl_wait();
   __syncthreads();
-  const int g = threadIdx.x / L, lane = threadIdx.x % L;
+  if ((int)threadIdx.x >= ch.cnt) return;
+  const SysDev& s = sys;
+  const int i = ch.beg + (int)threadIdx.x;
+  uint32_t xi[3] = {0u, 0u, 0u};
+  int c[3] = {0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    xi[k] = a.xr[k][i];
+    c[k] = cell_coord(s, k, xi[k]);
+  }
+  const uint32_t mi = a.meta[i];
+  const int moli = a.mol[i];
+  const int trbi = (mi >> 8) & 0xff, loci = (mi >> 16) & 0xff, tmi = mi >> 24;
+  const unsigned int pmask = s.partner[trbi];
+  const uint32_t bmask = tmi != 0xff ? a.tmpl[tmi].bondmask[loci] : 0u;
+  const float Rl2 = s.Rl2;
+  const int h1 = D > 1 ? s.halo[1] : 0;
+  const int h2 = D > 2 ? s.halo[2] : 0;
+  int rb[NRUN], re[NRUN];
+#pragma unroll
+  for (int q = 0; q < NROW; q++) {
+    const int dz = D == 3 ? q / 3 - 1 : 0;
+    const int dy = D >= 2 ? q % 3 - 1 : 0;
+    int row, lo0, hi0, lo1, hi1;
+    const bool ok = dy >= -h1 && dy <= h1 && dz >= -h2 && dz <= h2 &&
+                    row_runs<D>(s, c, dy, dz, row, lo0, hi0, lo1, hi1);
+    const int* cs = a.cell_start + s.c0 + row;
+    rb[2 * q] = ok ? cs[lo0] : 0;
+    re[2 * q] = ok ? cs[hi0 + 1] : 0;
+    const bool two = ok && hi1 >= lo1;
+    rb[2 * q + 1] = two ? cs[lo1] : 0;
+    re[2 * q + 1] = two ? cs[hi1 + 1] : 0;
+  }
+  // every run's candidate lines into L1 first (runs are short and contiguous)
+#pragma unroll
+  for (int q = 0; q < NRUN; q++) {
+    if (re[q] > rb[q]) {
+#pragma unroll
+      for (int k = 0; k < D; k++) {
+        prefetch_l1(a.xr[k] + rb[q]);
+        prefetch_l1(a.xr[k] + re[q] - 1);
+      }
+      prefetch_l1(a.meta + rb[q]);
+      prefetch_l1(a.meta + re[q] - 1);
+      prefetch_l1(a.mol + rb[q]);
+      prefetch_l1(a.mol + re[q] - 1);
+    }
+  }
   int* nbr = a.nbr_out;
   const int W = a.W, npad = a.npad;
-  for (int p = g; p < ch.cnt; p += LBLOCK / L) {
-    const int i = ch.beg + p;
-    const int cnt = row_scan<D, L>(sys, a, i, lane, [&](int e, int v) {
-      if (e < W) nbr[ell_index<TPP>(e, i, npad)] = v;
-    });
-    if (lane == 0) a.ncnt_out[i] = cnt;
+  int cnt = 0;
+#pragma unroll
+  for (int q = 0; q < NRUN; q++) {
+    for (int j0 = rb[q]; j0 < re[q]; j0 += U) {
+      uint32_t xx[U][3], mj[U];
+      int molj[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int jl = j0 + u < re[q] ? j0 + u : i;
+#pragma unroll
+        for (int k = 0; k < 3; k++) xx[u][k] = k < D ? a.xr[k][jl] : 0u;
+        mj[u] = a.meta[jl];
+        molj[u] = a.mol[jl];
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int j = j0 + u;
+        if (j >= re[q] || j == i) continue;
+        float r2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          const float d = (float)(int)(xx[u][k] - xi[k]) * s.unit_hi[k];
+          r2 += d * d;
+        }
+        if (!(r2 < Rl2)) continue;
+        bool hit;
+        int ent;
+        if (molj[u] == moli) {
+          hit = (bmask >> ((mj[u] >> 16) & 31)) & 1;
+          ent = j | LIST_SAME_MOL;
+        } else {
+          hit = (pmask >> ((mj[u] >> 8) & 0xff)) & 1;
+          ent = j;
+        }
+        if (hit) {
+          if (cnt < W) nbr[ell_index<TPP>(cnt, i, npad)] = ent;
+          cnt++;
+        }
+      }
+    }
   }
+  a.ncnt_out[i] = cnt;
 }
 
 // Reaction prefilter for the next step (sorted particle gi of type ti): the
