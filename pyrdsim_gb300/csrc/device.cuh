@@ -95,7 +95,8 @@ struct SysDev {
   unsigned long long seed;
   float fp[MAXT], npf[MAXT];      // dt*D and sqrt(2 dt D) per type
   unsigned int partner[MAXT];     // bit j of [i]: types i, j are partners
-  unsigned short ppair[MAXT * MAXT];  // first law << 5 | count, symmetric
+  unsigned short ppair[MAXT * MAXT];  // first law << 5 | count, symmetric;
+                                      // bit 15: one Lennard-Jones n = 6 law
   float prc2[MAXT * MAXT];        // largest guarded rc^2 of the pair's laws
   unsigned char rxmatch[MAXT * MAXT]; // bit r of [ti * MAXT + tj]: neighbour
                                       // reaction r has reactant ti and counts tj

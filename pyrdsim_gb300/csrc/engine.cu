@@ -803,14 +803,17 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         auto& v = by_pair[a * MAXT + b];
         if (v.empty()) continue;
         int first = (int)laws.size() - sd.law0;
-        if (first + (int)v.size() > 2047) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many pair laws"));
+        if (first + (int)v.size() > 1023) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many pair laws"));
         for (auto& L : v) {
           laws.push_back(L);
           R2 = std::max(R2, L.rc2_hi);
           sd.prc2[a * MAXT + b] = std::max(sd.prc2[a * MAXT + b], L.rc2_hi);
         }
         sd.prc2[b * MAXT + a] = sd.prc2[a * MAXT + b];
-        unsigned short code = (unsigned short)((first << 5) | (int)v.size());
+        // bit 15: the pair has a single Lennard-Jones law with n = 6 (the
+        // drift kernel evaluates it inline)
+        const bool lj6 = v.size() == 1 && v[0].law == RDSIM_LAW_LJ && v[0].n == 6;
+        unsigned short code = (unsigned short)((first << 5) | (int)v.size() | (lj6 ? 0x8000 : 0));
         sd.ppair[a * MAXT + b] = code;
         sd.ppair[b * MAXT + a] = code;
       }

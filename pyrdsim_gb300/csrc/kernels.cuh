@@ -125,7 +125,7 @@ __device__ inline float eval_pair(const PairLaw& L, float r2, float inv_r2) {
 template <int D>
 __device__ inline float pair_force(const SysDev& s, const PairLaw* laws, const Args& a, int gi,
                                    int gj, unsigned int pp, float r2) {
-  const int nl = pp & 31, l0 = pp >> 5;
+  const int nl = pp & 31, l0 = (pp >> 5) & 0x3ff;
   const float inv_r2 = __fdividef(1.0f, r2);
   float fr = 0.f;
   double dexact = -1.0;

@@ -498,7 +498,18 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
       const int tj = nb.m & 0xff;
       if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
       const unsigned int pp = s.ppair[ti * MAXT + tj];
-      const float fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
+      const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
+      float fr;
+      if ((pp & 0x8000u) && r2 < L0.rc2_lo) {
+        // a single Lennard-Jones n = 6 law, clear of its cutoff: the
+        // arithmetic of eval_pair inline
+        const float inv_r2 = __fdividef(1.0f, r2);
+        const float q = L0.c1 * inv_r2;
+        const float s6 = q * q * q;
+        fr = L0.c0 * s6 * (s6 - 1.0f) * inv_r2;
+      } else {
+        fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
+      }
 #pragma unroll
       for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
     });
