@@ -178,9 +178,10 @@ enum : int {
   F_INJECT = 8,                   // xi / u1 / u2 come from buffers
   F_RATES_ONLY = 16,              // reaction kernel: write total rates, no draw
   F_CHECK_SKIN = 32,
-  F_RX_NEXT = 64                  // drift kernel: copy the types forward and
+  F_RX_NEXT = 64,                 // drift kernel: copy the types forward and
                                   // list the particles whose reaction draw of
                                   // the next step may succeed
+  F_RX_HERE = 128                 // list builder: the same for its own step
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------

@@ -293,9 +293,12 @@ void launch_step_kernel(rdsim_handle* h, bool react, const Args& a) {
 
 unsigned nblk(int n, int b = 256) { return (unsigned)((n + b - 1) / b); }
 
-int rebuild(rdsim_handle* h) {
+// `prefilter`: the list builder also runs the reaction prefilter of `step`
+// (then the reaction kernel of that step visits the listed particles only);
+// `rel`: step numbers are offsets from the device counter (graph capture).
+int rebuild(rdsim_handle* h, long long step = 0, bool prefilter = false, bool rel = false) {
   const int n = h->N;
-  ProfScope ps(h, P_REBUILD, 6);
+  ProfScope ps(h, P_REBUILD, h->ncells <= SCAN1_T * SCAN1_I ? 5 : 6);
   uint32_t* const* x = h->xh[h->cx];
   if (h->D == 2)
     launch(k_bin<2>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
@@ -303,8 +306,12 @@ int rebuild(rdsim_handle* h) {
     launch(k_bin<3>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
   else
     launch(k_bin<1>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
-  launch(k_scan_partial, h->nscan, 256, h->stream, h->cell_count, h->ncells, h->bsum);
-  launch(k_scan_final, h->nscan, 256, h->stream, h->cell_count, h->ncells, h->bsum, h->cell_start);
+  if (h->ncells <= SCAN1_T * SCAN1_I) {
+    launch(k_scan_one, 1, SCAN1_T, h->stream, h->cell_count, h->ncells, h->cell_start);
+  } else {
+    launch(k_scan_partial, h->nscan, 256, h->stream, h->cell_count, h->ncells, h->bsum);
+    launch(k_scan_final, h->nscan, 256, h->stream, h->cell_count, h->ncells, h->bsum, h->cell_start);
+  }
   launch(k_scatter, nblk(n), 256, h->stream, h->cell_of, h->rank_of, h->cell_start, n, h->tmp,
          h->cell_count, h->ncells);
   Args a = make_args(h);
@@ -319,7 +326,10 @@ int rebuild(rdsim_handle* h) {
   h->cx = 1 - h->cx;
   h->cm = 1 - h->cm;
   h->co = 1 - h->co;
-  const Args b = make_args(h);
+  Args b = make_args(h);
+  b.step = step;
+  b.step_base = rel ? h->step_dev : nullptr;
+  b.flags = prefilter ? F_RX_HERE : 0;
   if (h->D == 2) launch_nlist<2>(h, b);
   else if (h->D == 3) launch_nlist<3>(h, b);
   else launch_nlist<1>(h, b);
@@ -512,10 +522,11 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
     std::memcpy(before, h->nlaunch, sizeof before);
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = rebuild(h);
+    int rc = rebuild(h, 0, pre, true);
     for (int i = 0; i < h->freq && !rc; i++) {
-      // the prefilter flags of step i come from the drift kernel of step i - 1
-      const bool flagged = pre && i > 0, flag_next = pre && i + 1 < h->freq;
+      // the prefiltered particles of step i are listed by the list builder
+      // (i = 0) or by the drift kernel of step i - 1
+      const bool flagged = pre, flag_next = pre && i + 1 < h->freq;
       if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
       if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
     }
@@ -1231,8 +1242,8 @@ int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi
       continue;
     }
     if (s % h->freq == 0) {
-      if ((rc = rebuild(h))) return rc;
-      flagged = false;  // flags are in the order before the re-sort
+      if ((rc = rebuild(h, s, pre))) return rc;
+      flagged = pre;  // the builder listed this step's candidates
     }
     if (h->has_rx) {
       if ((rc = react(h, s, kf, du1 ? du1 + (size_t)q * N : nullptr,

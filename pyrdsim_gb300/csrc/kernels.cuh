@@ -613,6 +613,59 @@ __global__ void k_bin(const SysDev* sysv, const int* sid, const uint32_t* x0, co
 constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = 256 * SCAN_ITEMS;
 
+// The same in one CTA when n <= SCAN1_T * SCAN1_I (one launch instead of
+// two).  Warp w owns the contiguous segment [w * seg, (w + 1) * seg), loaded
+// 32 items per instruction (coalesced) into registers; the warp totals are
+// scanned across the CTA, then every warp scans its segment with shuffles.
+constexpr int SCAN1_T = 1024;
+constexpr int SCAN1_I = 32;
+
+__global__ void __launch_bounds__(SCAN1_T) k_scan_one(const int* count, int n, int* start) {
+  pdl_trigger();
+  pdl_wait();
+  __shared__ int ws[SCAN1_T / 32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int seg = (((n + SCAN1_T / 32 - 1) / (SCAN1_T / 32)) + 31) & ~31;  // items per warp
+  const int base = w * seg;
+  int v[SCAN1_I], sum = 0;
+#pragma unroll
+  for (int it = 0; it < SCAN1_I; it++) {
+    const int q = base + it * 32 + lane;
+    v[it] = (it * 32 < seg && q < n) ? count[q] : 0;
+    sum += v[it];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) ws[w] = sum;
+  __syncthreads();
+  if (w == 0) {
+    const int x0 = ws[lane];
+    int x = x0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    ws[lane] = x - x0;  // exclusive
+    if (lane == 31 && tid == 31) start[n] = x;  // the total
+  }
+  __syncthreads();
+  int run = ws[w];
+#pragma unroll
+  for (int it = 0; it < SCAN1_I; it++) {
+    if (it * 32 >= seg) break;
+    int x = v[it];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const int q = base + it * 32 + lane;
+    if (q < n) start[q] = run + x - v[it];
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
+}
+
 __global__ void k_scan_partial(const int* count, int n, int* bsum) {
   pdl_trigger();
   pdl_wait();

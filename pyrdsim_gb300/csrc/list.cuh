@@ -315,11 +315,36 @@ __device__ inline void for_entries(const SysDev& s, const Args& a, int i, int la
   }
 }
 
+// Reaction prefilter of a step (sorted particle gi of type ti): the
+// float64 total propensity of that step grows monotonically with every
+// neighbour count, so rxA + rxB * (list entries), with a relative margin far
+// above the rounding of the reference's repeated additions, bounds it from
+// above.  If dt times the bound does not exceed the step's u1 (the same
+// counter-based draw the reaction kernel makes), the draw `dt * total > u1`
+// (pyrdsim.pyx:2211-2213) cannot succeed and the particle keeps its type.
+// The bound and the comparison are float32: rxAf, rxBf and dtf are rounded
+// up, the relative margin 1e-5 covers the float32 rounding, and the uniform
+// is replaced by the lower bound of its top 24 bits.  Returns true when the
+// draw may succeed (cnt: list entries, pid: caller index, w0: the tag-0
+// words of the next step).
+template <int D>
+__device__ inline bool rx_may_react(const SysDev& s, int ti, int cnt, int pid, long long step,
+                                    const U4* w0) {
+  if (!((s.rx_any_mask >> ti) & 1)) return false;
+  uint32_t hi, lo;
+  u1_words<D>(s.seed, step, pid, w0, hi, lo);
+  float u1lo, u1hi;
+  uniform_bounds(hi, u1lo, u1hi);
+  const float ub = (s.rxAf[ti] + s.rxBf[ti] * (float)cnt) * (1.0f + 1e-5f);
+  return s.dtf * ub > u1lo;
+}
+
 // Rebuild: every particle's list row and entry count, one thread per
 // particle and one CTA per run of LBLOCK / TPP particles.  The thread walks
 // the runs of its cell neighbourhood in candidate order (the order row_scan
 // uses), four candidates per batch of loads, and appends the listed pairs
-// within the list radius.
+// within the list radius.  With F_RX_HERE it also runs the reaction
+// prefilter of its step with the fresh entry counts.
 template <int D, int TPP>
 __global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
   constexpr int PER = LBLOCK / TPP;
@@ -337,7 +362,10 @@ __global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
   }
   pdl_wait();
   __syncthreads();
-  if ((int)threadIdx.x >= ch.cnt) return;
+  const bool valid = (int)threadIdx.x < ch.cnt;
+  int4 rec = make_int4(0, 0, 0, 0);
+  bool listed = false;
+  if (valid) {
   const SysDev& s = sys;
   const int i = ch.beg + (int)threadIdx.x;
   uint32_t xi[3] = {0u, 0u, 0u};
@@ -429,31 +457,25 @@ __global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
     }
   }
   a.ncnt_out[i] = cnt;
+  if (a.flags & F_RX_HERE) {  // reaction prefilter of this step (see rx_may_react)
+    a.meta_out[i] = mi;
+    rec = make_int4(i, (int)mi, cnt, a.pid[i]);
+    listed = rx_may_react<D>(s, (int)(mi & 0xff), cnt, rec.w, eff_step(a), nullptr);
+  }
+  }
+  if (a.flags & F_RX_HERE) {
+    const unsigned int bal = __ballot_sync(0xffffffffu, listed);
+    if (bal) {
+      const int l32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
+      const int p = (int)(eff_step(a) & 1);
+      int base = 0;
+      if (l32 == leader) base = atomicAdd(a.rx_count + p, __popc(bal));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (listed) a.rx_list[(size_t)p * a.npad + base + __popc(bal & ((1u << l32) - 1u))] = rec;
+    }
+  }
 }
 
-// Reaction prefilter for the next step (sorted particle gi of type ti): the
-// float64 total propensity of that step grows monotonically with every
-// neighbour count, so rxA + rxB * (list entries), with a relative margin far
-// above the rounding of the reference's repeated additions, bounds it from
-// above.  If dt times the bound does not exceed the next step's u1 (the same
-// counter-based draw the reaction kernel makes), the draw `dt * total > u1`
-// (pyrdsim.pyx:2211-2213) cannot succeed and the particle keeps its type.
-// The bound and the comparison are float32: rxAf, rxBf and dtf are rounded
-// up, the relative margin 1e-5 covers the float32 rounding, and the uniform
-// is replaced by the lower bound of its top 24 bits.  Returns true when the
-// draw may succeed (cnt: list entries, pid: caller index, w0: the tag-0
-// words of the next step).
-template <int D>
-__device__ inline bool rx_may_react(const SysDev& s, const Args& a, int ti, int cnt, int pid,
-                                    const U4& w0) {
-  if (!((s.rx_any_mask >> ti) & 1)) return false;
-  uint32_t hi, lo;
-  u1_words<D>(s.seed, eff_em_step(a), pid, &w0, hi, lo);
-  float u1lo, u1hi;
-  uniform_bounds(hi, u1lo, u1hi);
-  const float ub = (s.rxAf[ti] + s.rxBf[ti] * (float)cnt) * (1.0f + 1e-5f);
-  return s.dtf * ub > u1lo;
-}
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
 // list entries (pyrdsim.pyx:1988-2030).  Phase B: one thread per particle
@@ -545,7 +567,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     if (a.flags & F_RX_NEXT) {
       a.meta_out[ib] = mb;  // the next step's types, unless its draw succeeds
       rec = make_int4(ib, (int)mb, a.ncnt[ib], pid);
-      listed = rx_may_react<D>(s, a, (int)(mb & 0xff), rec.z, pid, w0);
+      listed = rx_may_react<D>(s, (int)(mb & 0xff), rec.z, pid, eff_em_step(a), &w0);
     }
   }
   if (a.flags & F_RX_NEXT) {
