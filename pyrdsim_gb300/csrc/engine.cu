@@ -278,7 +278,7 @@ void launch_listed(rdsim_handle* h, unsigned g, const Args& a) {
 template <int D>
 void launch_nlist(rdsim_handle* h, const Args& a) {
   const dim3 grid((unsigned)h->chunks_h.size());
-  const unsigned per = (unsigned)(LBLOCK / h->ltpp);
+  const unsigned per = (unsigned)(LBLOCK / h->ltpp * (D == 1 ? 1 : 3));
   if (h->ltpp == 1) launch(k_nlist<D, 1>, grid, per, h->stream, a);
   else if (h->ltpp == 2) launch(k_nlist<D, 2>, grid, per, h->stream, a);
   else if (h->ltpp == 8) launch(k_nlist<D, 8>, grid, per, h->stream, a);

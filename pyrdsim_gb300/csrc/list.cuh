@@ -339,35 +339,41 @@ __device__ inline bool rx_may_react(const SysDev& s, int ti, int cnt, int pid, l
   return s.dtf * ub > u1lo;
 }
 
-// Rebuild: every particle's list row and entry count, one thread per
-// particle and one CTA per run of LBLOCK / TPP particles.  The thread walks
-// the runs of its cell neighbourhood in candidate order (the order row_scan
-// uses), four candidates per batch of loads, and appends the listed pairs
-// within the list radius.  With F_RX_HERE it also runs the reaction
-// prefilter of its step with the fresh entry counts.
+// Rebuild: every particle's list row and entry count.  NT threads per
+// particle (3 for D >= 2: one per row of cells in 2D, one per three rows in
+// 3D) scan their rows' runs in candidate order, four candidates per batch of
+// loads, into shared-memory buffers; the buffers are then concatenated in row
+// order (the order row_scan uses), so the row does not depend on NT.  A
+// thread whose rows hold more than BCAP listed pairs rescans them to write
+// the rest.  With F_RX_HERE the first thread of each particle also runs the
+// reaction prefilter of its step with the fresh entry count.
 template <int D, int TPP>
-__global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
+__global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Args a) {
   constexpr int PER = LBLOCK / TPP;
+  constexpr int NT = D == 1 ? 1 : 3;
+  constexpr int NTH = PER * NT;
   constexpr int NROW = D == 3 ? 9 : (D == 2 ? 3 : 1);
-  constexpr int NRUN = 2 * NROW;
+  constexpr int RPT = NROW / NT;  // rows per thread
+  constexpr int NRUN = 2 * RPT;
   constexpr int U = 4;
+  constexpr int BCAP = 24;
   __shared__ SysDev sys;
+  __shared__ int sbuf[NTH][BCAP];
+  __shared__ int scnt[NTH];
   pdl_trigger();
   const Chunk ch = chunk_at<PER>(a, (int)blockIdx.x);
   {
     constexpr int NS = (int)(sizeof(SysDev) / 4);
-    WordLoad<NS, PER> ls;
+    WordLoad<NS, NTH> ls;
     ls.load(reinterpret_cast<const int*>(&a.sys[ch.sys]), NS);
     ls.store(reinterpret_cast<int*>(&sys), NS);
   }
   pdl_wait();
   __syncthreads();
-  const bool valid = (int)threadIdx.x < ch.cnt;
-  int4 rec = make_int4(0, 0, 0, 0);
-  bool listed = false;
-  if (valid) {
   const SysDev& s = sys;
-  const int i = ch.beg + (int)threadIdx.x;
+  const int tid = (int)threadIdx.x, pp = tid / NT, t = tid % NT;
+  const bool valid = pp < ch.cnt;
+  const int i = ch.beg + (valid ? pp : 0);
   uint32_t xi[3] = {0u, 0u, 0u};
   int c[3] = {0, 0, 0};
 #pragma unroll
@@ -385,83 +391,94 @@ __global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
   const int h2 = D > 2 ? s.halo[2] : 0;
   int rb[NRUN], re[NRUN];
 #pragma unroll
-  for (int q = 0; q < NROW; q++) {
+  for (int r = 0; r < RPT; r++) {
+    const int q = t * RPT + r;
     const int dz = D == 3 ? q / 3 - 1 : 0;
     const int dy = D >= 2 ? q % 3 - 1 : 0;
     int row, lo0, hi0, lo1, hi1;
-    const bool ok = dy >= -h1 && dy <= h1 && dz >= -h2 && dz <= h2 &&
+    const bool ok = valid && dy >= -h1 && dy <= h1 && dz >= -h2 && dz <= h2 &&
                     row_runs<D>(s, c, dy, dz, row, lo0, hi0, lo1, hi1);
     const int* cs = a.cell_start + s.c0 + row;
-    rb[2 * q] = ok ? cs[lo0] : 0;
-    re[2 * q] = ok ? cs[hi0 + 1] : 0;
+    rb[2 * r] = ok ? cs[lo0] : 0;
+    re[2 * r] = ok ? cs[hi0 + 1] : 0;
     const bool two = ok && hi1 >= lo1;
-    rb[2 * q + 1] = two ? cs[lo1] : 0;
-    re[2 * q + 1] = two ? cs[hi1 + 1] : 0;
+    rb[2 * r + 1] = two ? cs[lo1] : 0;
+    re[2 * r + 1] = two ? cs[hi1 + 1] : 0;
   }
-  // every run's candidate lines into L1 first (runs are short and contiguous)
+  // the listed pairs of this thread's rows, in candidate order: emit(k, entry)
+  auto scan_rows = [&](auto&& emit) {
+    int k = 0;
 #pragma unroll
-  for (int q = 0; q < NRUN; q++) {
-    if (re[q] > rb[q]) {
+    for (int q = 0; q < NRUN; q++) {
+      for (int j0 = rb[q]; j0 < re[q]; j0 += U) {
+        uint32_t xx[U][3], mj[U];
+        int molj[U];
 #pragma unroll
-      for (int k = 0; k < D; k++) {
-        prefetch_l1(a.xr[k] + rb[q]);
-        prefetch_l1(a.xr[k] + re[q] - 1);
-      }
-      prefetch_l1(a.meta + rb[q]);
-      prefetch_l1(a.meta + re[q] - 1);
-      prefetch_l1(a.mol + rb[q]);
-      prefetch_l1(a.mol + re[q] - 1);
-    }
-  }
-  int* nbr = a.nbr_out;
-  const int W = a.W, npad = a.npad;
-  int cnt = 0;
+        for (int u = 0; u < U; u++) {
+          const int jl = j0 + u < re[q] ? j0 + u : i;
 #pragma unroll
-  for (int q = 0; q < NRUN; q++) {
-    for (int j0 = rb[q]; j0 < re[q]; j0 += U) {
-      uint32_t xx[U][3], mj[U];
-      int molj[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int jl = j0 + u < re[q] ? j0 + u : i;
-#pragma unroll
-        for (int k = 0; k < 3; k++) xx[u][k] = k < D ? a.xr[k][jl] : 0u;
-        mj[u] = a.meta[jl];
-        molj[u] = a.mol[jl];
-      }
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int j = j0 + u;
-        if (j >= re[q] || j == i) continue;
-        float r2 = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; k++) {
-          const float d = (float)(int)(xx[u][k] - xi[k]) * s.unit_hi[k];
-          r2 += d * d;
+          for (int d = 0; d < 3; d++) xx[u][d] = d < D ? a.xr[d][jl] : 0u;
+          mj[u] = a.meta[jl];
+          molj[u] = a.mol[jl];
         }
-        if (!(r2 < Rl2)) continue;
-        bool hit;
-        int ent;
-        if (molj[u] == moli) {
-          hit = (bmask >> ((mj[u] >> 16) & 31)) & 1;
-          ent = j | LIST_SAME_MOL;
-        } else {
-          hit = (pmask >> ((mj[u] >> 8) & 0xff)) & 1;
-          ent = j;
-        }
-        if (hit) {
-          if (cnt < W) nbr[ell_index<TPP>(cnt, i, npad)] = ent;
-          cnt++;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int j = j0 + u;
+          if (j >= re[q] || j == i) continue;
+          float r2 = 0.f;
+#pragma unroll
+          for (int d = 0; d < D; d++) {
+            const float dd = (float)(int)(xx[u][d] - xi[d]) * s.unit_hi[d];
+            r2 += dd * dd;
+          }
+          if (!(r2 < Rl2)) continue;
+          bool hit;
+          int ent;
+          if (molj[u] == moli) {
+            hit = (bmask >> ((mj[u] >> 16) & 31)) & 1;
+            ent = j | LIST_SAME_MOL;
+          } else {
+            hit = (pmask >> ((mj[u] >> 8) & 0xff)) & 1;
+            ent = j;
+          }
+          if (hit) emit(k++, ent);
         }
       }
     }
+    return k;
+  };
+  const int cnt = scan_rows([&](int k, int ent) {
+    if (k < BCAP) sbuf[tid][k] = ent;
+  });
+  scnt[tid] = cnt;
+  __syncthreads();
+  int off = 0, total = 0;
+#pragma unroll
+  for (int u = 0; u < NT; u++) {
+    const int cu = scnt[pp * NT + u];
+    if (u < t) off += cu;
+    total += cu;
   }
-  a.ncnt_out[i] = cnt;
-  if (a.flags & F_RX_HERE) {  // reaction prefilter of this step (see rx_may_react)
-    a.meta_out[i] = mi;
-    rec = make_int4(i, (int)mi, cnt, a.pid[i]);
-    listed = rx_may_react<D>(s, (int)(mi & 0xff), cnt, rec.w, eff_step(a), nullptr);
-  }
+  int4 rec = make_int4(0, 0, 0, 0);
+  bool listed = false;
+  if (valid) {
+    int* nbr = a.nbr_out;
+    const int W = a.W, npad = a.npad;
+    const int nb = min(cnt, BCAP);
+    for (int k = 0; k < nb; k++)
+      if (off + k < W) nbr[ell_index<TPP>(off + k, i, npad)] = sbuf[tid][k];
+    if (cnt > BCAP && off + BCAP < W)
+      scan_rows([&](int k, int ent) {
+        if (k >= BCAP && off + k < W) nbr[ell_index<TPP>(off + k, i, npad)] = ent;
+      });
+    if (t == 0) {
+      a.ncnt_out[i] = total;
+      if (a.flags & F_RX_HERE) {  // reaction prefilter of this step (see rx_may_react)
+        a.meta_out[i] = mi;
+        rec = make_int4(i, (int)mi, total, a.pid[i]);
+        listed = rx_may_react<D>(s, (int)(mi & 0xff), total, rec.w, eff_step(a), nullptr);
+      }
+    }
   }
   if (a.flags & F_RX_HERE) {
     const unsigned int bal = __ballot_sync(0xffffffffu, listed);
@@ -475,7 +492,6 @@ __global__ void __launch_bounds__(LBLOCK / TPP) k_nlist(Args a) {
     }
   }
 }
-
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
 // list entries (pyrdsim.pyx:1988-2030).  Phase B: one thread per particle
