@@ -224,6 +224,52 @@ int rdsim_get_pairs_static(rdsim_handle* h, int32_t sys, int32_t* pairs,
  * reference's cell geometry (pyrdsim.pyx:1415-1446, 1506-1508). */
 int rdsim_get_cell_ids(rdsim_handle* h, int32_t sys, int32_t* cell_ids);
 
+/* ---- observables (no reference counterpart except min_distance) --------
+ * Float64 reductions over system `sys` at the current state, computed on the
+ * device.  Energies are the potentials whose derivatives are the
+ * reference's force laws (pyrdsim.pyx:1068-1145, 2037-2066), each truncated
+ * (not shifted) where its force stops:
+ *   lj                U = u0 [(r0/r)^2n - 2 (r0/r)^n]            r <= rc
+ *   tanh              U = (u0/2) [tanh((r - r0)/a) - 1]          r <= rc
+ *   yukawa            U = u0 exp(-r/r0) / r                      r <= rc
+ *   harmonic          U = u0 r^2 / 2                             r <= rc
+ *   piecewise_linear  U = (u0/dr) (r - r0) on [r0 - dr, r0], -u0 below
+ *   tanh wall         U = (u0/2) [tanh((x_d - r0)/a) - 1]
+ *   9-3 wall          U = u0 [(2/15)(r0/y)^9 - (r0/y)^3]         y <= rc
+ *   bond              U = U0 (d - r0)^2 / 2
+ *   angle             U = k (theta - theta0)^2 / 2  (k in the deck's
+ *                                                    per-radian^2 units)
+ * Pair terms run over the pairs whose forces the drift applies: listed
+ * pairs of different molecules, each law of their (small, large) type pair
+ * within its cutoff.  virial = sum over those pairs and the bonds of
+ * -r dU/dr (angle terms contribute nothing, walls are external).
+ * min_distance is the smallest distance between listed interaction or
+ * reaction partners of different molecules: pairs within the Verlet-list
+ * radius (interaction range + skin) at the last rebuild; +inf if there is
+ * none.  At a rebuild it equals the reference's min_dist
+ * (pyrdsim.pyx:1640-1652) whenever that is below the interaction range. */
+typedef struct {
+  double pair_energy, wall_energy, bond_energy, angle_energy;
+  double virial;
+  double min_distance;
+  int64_t n_pairs;      /* particle pairs within the cutoff of one of their
+                           pair laws                                        */
+  int64_t n_particles;
+  int64_t type_counts[RDSIM_MAX_TYPES];  /* particles of each current type */
+} rdsim_observables;
+int rdsim_get_observables(rdsim_handle* h, int32_t sys, rdsim_observables* out);
+
+/* Pair-distance histogram of system `sys` (for g(r)): counts[b] += 1 for
+ * every unordered particle pair of types {type_a, type_b} (-1: any type)
+ * at float64 distance r < r_max (minimum image in periodic dimensions),
+ * b = floor(r / (r_max / n_bins)).  With RDSIM_RDF_OTHER_MOLECULES only
+ * pairs of different molecules count.  r_max must not exceed half of any
+ * periodic box length; 1 <= n_bins <= 16384.  counts[n_bins] is
+ * overwritten. */
+enum { RDSIM_RDF_OTHER_MOLECULES = 1 };
+int rdsim_get_rdf(rdsim_handle* h, int32_t sys, int32_t type_a, int32_t type_b,
+                  double r_max, int32_t n_bins, int32_t flags, int64_t* counts);
+
 /* Step counter (the reference's `step` argument of integration_step); the
  * next rdsim_step performs step counter+1.  Sets it for append mode. */
 int rdsim_get_step(rdsim_handle* h, int64_t* step);
@@ -261,7 +307,7 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
  * bracketed by CUDA events on the handle's stream and its device time summed
  * per class: 0 = drift (k_force_l), 1 = reactions (k_react_l,
  * k_react_listed), 2 = stand-alone Euler-Maruyama (k_em), 3 = cell-list and
- * Verlet-list rebuild (6 kernels), 4 = hooks. */
+ * Verlet-list rebuild (6 kernels), 4 = hooks and observables. */
 #define RDSIM_PROFILE_CLASSES 5
 typedef struct {
   int64_t launches[RDSIM_PROFILE_CLASSES];

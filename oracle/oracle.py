@@ -59,6 +59,9 @@ def lib():
                                        C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                        C.POINTER(C.c_int64)]
         L.oracle_set_step.argtypes = [vp, C.c_int64]
+        L.oracle_get_observables.argtypes = [vp, C.POINTER(abi.Observables)]
+        L.oracle_get_rdf.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                     C.c_int32, C.POINTER(C.c_int64)]
         L.oracle_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -142,6 +145,19 @@ class Oracle:
         c = np.empty((self.N, self.D), dtype=np.int32)
         _check(lib().oracle_get_cell_ids(self.h, abi.iptr(c)))
         return c
+
+    def observables(self):
+        o = abi.Observables()
+        _check(lib().oracle_get_observables(self.h, C.byref(o)))
+        return o.as_dict()
+
+    def rdf_counts(self, r_max, n_bins=100, type_a=-1, type_b=-1, other_molecules=False):
+        counts = np.zeros(int(n_bins), dtype=np.int64)
+        flags = abi.RDF_OTHER_MOLECULES if other_molecules else 0
+        _check(lib().oracle_get_rdf(self.h, int(type_a), int(type_b), float(r_max),
+                                    int(n_bins), flags,
+                                    counts.ctypes.data_as(C.POINTER(C.c_int64))))
+        return counts
 
     def min_dist(self):
         v = C.c_double()

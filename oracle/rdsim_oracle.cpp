@@ -596,4 +596,108 @@ int oracle_get_error(oracle_handle* h, int32_t* code, int64_t* particle, int32_t
 
 int oracle_set_step(oracle_handle* h, int64_t step) { h->step = step; return 0; }
 
+// Potentials of the force laws above, truncated where the force stops
+// (observables; the reference has none).  Returns U; f = dU/dr as law().
+static double potential(const rdsim_interaction& it, double r) {
+  switch (it.law) {
+    case RDSIM_LAW_LJ: {
+      double s = std::pow(it.r0 / r, (double)it.n);
+      return it.u0 * s * (s - 2.);
+    }
+    case RDSIM_LAW_TANH:
+      return it.u0 / 2. * (std::tanh((r - it.r0) / it.a) - 1.);
+    case RDSIM_LAW_YUKAWA:
+      return it.u0 * std::exp(-r / it.r0) / r;
+    case RDSIM_LAW_HARMONIC:
+      return it.u0 * r * r / 2.;
+    case RDSIM_LAW_PIECEWISE_LINEAR:
+      if (r < it.r0 - it.dr) return -it.u0;
+      return it.u0 / it.dr * (r - it.r0);
+  }
+  return 0.0;
+}
+
+// Energies, virial and counts of rdsim_get_observables over the oracle's own
+// neighbour list, in the loop order of update_drifts (pyx:1941-2067).
+int oracle_get_observables(oracle_handle* h, rdsim_observables* out) {
+  std::memset(out, 0, sizeof *out);
+  const int N = h->N, D = h->D;
+  std::set<uint64_t> in_range;
+  for (const rdsim_interaction& it : h->inter) {
+    if (it.law == RDSIM_LAW_WALL || it.law == RDSIM_LAW_WALL93) {
+      for (int i = 0; i < N; i++) {
+        if (h->types[i] != it.type_a) continue;
+        double y = h->x[(size_t)i * D + it.type_b];
+        if (it.law == RDSIM_LAW_WALL) {
+          out->wall_energy += it.u0 / 2. * (std::tanh((y - it.r0) / it.a) - 1.);
+        } else if (!(y > it.rc)) {
+          double q = it.r0 / y, q3 = q * q * q, q9 = q3 * q3 * q3;
+          out->wall_energy += it.u0 * (2. / 15. * q9 - q3);
+        }
+      }
+      continue;
+    }
+    double rc = (it.law == RDSIM_LAW_PIECEWISE_LINEAR) ? it.r0 : it.rc;
+    for (int i1 = 0; i1 < N; i1++) {
+      for (int i2 : h->nl[i1]) {
+        if (h->mol[3 * i1] == h->mol[3 * i2]) continue;
+        int p1 = std::min(h->types[i1], h->types[i2]);
+        int p2 = std::max(h->types[i1], h->types[i2]);
+        if (!(p1 == it.type_a && p2 == it.type_b)) continue;
+        double r = h->dxx(i1, i2);
+        if (r > rc) continue;
+        out->pair_energy += potential(it, r);
+        out->virial += -r * oracle_handle::law(it, r);
+        in_range.insert(h->key(std::min(i1, i2), std::max(i1, i2)));
+      }
+    }
+  }
+  for (const BondF& b : h->bonds) {
+    double d = h->dxx(b.i1, b.i2);
+    out->bond_energy += b.k * (d - b.r0) * (d - b.r0) / 2.;
+    out->virial += -d * b.k * (d - b.r0);
+  }
+  for (const AngleF& an : h->angles) {
+    double c = 0.;
+    for (int k = 0; k < D; k++) c += h->hat(an.i2, an.i1, k) * h->hat(an.i2, an.i3, k);
+    double theta = c <= -1. ? M_PI : (c >= 1. ? 0. : std::acos(c));
+    out->angle_energy += an.k0 * (theta - an.theta0) * (theta - an.theta0) / 2.;
+  }
+  out->min_distance = h->min_dist;
+  out->n_pairs = (int64_t)in_range.size();
+  out->n_particles = N;
+  for (int i = 0; i < N; i++)
+    if (h->types[i] >= 0 && h->types[i] < RDSIM_MAX_TYPES) out->type_counts[h->types[i]] += 1;
+  return 0;
+}
+
+// Pair-distance histogram of rdsim_get_rdf over all pairs (i < j).
+int oracle_get_rdf(oracle_handle* h, int32_t type_a, int32_t type_b, double r_max,
+                   int32_t n_bins, int32_t flags, int64_t* counts) {
+  if (n_bins < 1 || !(r_max > 0)) return fail(RDSIM_ERR_ARG, "bad histogram");
+  const int N = h->N, D = h->D;
+  const double w = r_max / n_bins;
+  auto is = [](int t, int want) { return want < 0 || t == want; };
+  for (int b = 0; b < n_bins; b++) counts[b] = 0;
+  for (int i = 0; i < N; i++) {
+    int ti = h->types[i];
+    for (int j = i + 1; j < N; j++) {
+      int tj = h->types[j];
+      if (!((is(ti, type_a) && is(tj, type_b)) || (is(ti, type_b) && is(tj, type_a)))) continue;
+      if ((flags & RDSIM_RDF_OTHER_MOLECULES) && h->mol[3 * i] == h->mol[3 * j]) continue;
+      double d2 = 0.;
+      for (int k = 0; k < D; k++) {
+        double v = h->x[(size_t)j * D + k] - h->x[(size_t)i * D + k];
+        if (h->periodic[k] > 0) v = v - h->L[k] * std::round(v / h->L[k]);
+        d2 += v * v;
+      }
+      double r = std::sqrt(d2);
+      if (!(r < r_max)) continue;
+      int b = (int)std::floor(r / w);
+      counts[b < n_bins ? b : n_bins - 1] += 1;
+    }
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -46,6 +46,11 @@ int oracle_get_min_dist(oracle_handle* h, double* min_dist);
 int oracle_get_error(oracle_handle* h, int32_t* code, int64_t* particle,
                      int32_t* dim, double* value, int64_t* step);
 int oracle_set_step(oracle_handle* h, int64_t step);
+/* rdsim_get_observables / rdsim_get_rdf restated over the oracle's state and
+ * neighbour list (min_distance: min_dist of the last calculate_distances). */
+int oracle_get_observables(oracle_handle* h, rdsim_observables* out);
+int oracle_get_rdf(oracle_handle* h, int32_t type_a, int32_t type_b, double r_max,
+                   int32_t n_bins, int32_t flags, int64_t* counts);
 const char* oracle_last_error(void);
 
 #ifdef __cplusplus

@@ -121,6 +121,23 @@ class Info(C.Structure):
                 ("pad", C.c_int32)]
 
 
+RDF_OTHER_MOLECULES = 1
+RDF_MAX_BINS = 8192
+
+
+class Observables(C.Structure):
+    _fields_ = [("pair_energy", C.c_double), ("wall_energy", C.c_double),
+                ("bond_energy", C.c_double), ("angle_energy", C.c_double),
+                ("virial", C.c_double), ("min_distance", C.c_double),
+                ("n_pairs", C.c_int64), ("n_particles", C.c_int64),
+                ("type_counts", C.c_int64 * MAX_TYPES)]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "type_counts"}
+        d["type_counts"] = list(self.type_counts)
+        return d
+
+
 PROFILE_CLASSES = 5
 PROFILE_NAMES = ["force", "react", "em", "rebuild", "hook"]
 

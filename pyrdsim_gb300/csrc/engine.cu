@@ -21,6 +21,7 @@
 #include "device.cuh"
 #include "kernels.cuh"
 #include "list.cuh"
+#include "observe.cuh"
 
 using namespace rd;
 
@@ -83,6 +84,15 @@ struct rdsim_handle {
   TmplDev* tmpl_d = nullptr;
   TermDev* terms_d = nullptr;
   int* atomterm_d = nullptr;
+  // float64 parameters of the same tables (observables)
+  rdsim_interaction* olaws_d = nullptr;
+  rdsim_interaction* owalls_d = nullptr;
+  rdsim_term* oterms_d = nullptr;
+  // observables scratch, allocated by the first call that needs it
+  double* obs_part = nullptr;          // [obs_cap][OBS_NSUM] CTA partials, then sums
+  unsigned long long* obs_counts = nullptr;  // [1 + MAXT]
+  int obs_cap = 0;
+  unsigned long long* rdf_counts = nullptr;  // [RDF_MAX_BINS]
   int ncells = 0, nscan = 0;
   int *cell_count = nullptr, *cell_start = nullptr, *bsum = nullptr;
   // Verlet-list kernels
@@ -578,6 +588,8 @@ void free_all(rdsim_handle* h) {
   for (int k = 0; k < 3; k++) { F(h->xr[k]); F(h->drift[k]); }
   F(h->rates); F(h->xbuf); F(h->tbuf); F(h->err); F(h->cl_d);
   F(h->inj_xi); F(h->inj_u1); F(h->inj_u2); F(h->traj_x); F(h->traj_t);
+  F(h->olaws_d); F(h->owalls_d); F(h->oterms_d); F(h->obs_part); F(h->obs_counts);
+  F(h->rdf_counts);
   for (auto& p : h->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -638,6 +650,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   std::vector<RxDev> rxs;
   std::vector<TmplDev> tmpls;
   std::vector<TermDev> terms;
+  std::vector<rdsim_interaction> olaws, owalls;  // float64 copies, same order
+  std::vector<rdsim_term> oterms;
   std::vector<int> atomterm;
   std::vector<double> x_all;
   std::vector<int> t_all;
@@ -735,6 +749,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     sd.wall0 = (int)walls.size();
     double R = 0;
     std::vector<std::vector<PairLaw>> by_pair(MAXT * MAXT);
+    std::vector<std::vector<rdsim_interaction>> by_pair_o(MAXT * MAXT);
     for (int q = 0; q < S.n_interactions; q++) {
       const rdsim_interaction& it = S.interactions[q];
       if (it.law == RDSIM_LAW_WALL || it.law == RDSIM_LAW_WALL93) {
@@ -759,6 +774,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
           w.rc_hi = (float)(it.rc * (1 + 1e-5) + 4 * sd.unit_hi[w.dim]);
         }
         walls.push_back(w);
+        owalls.push_back(it);
         continue;
       }
       if (it.law < RDSIM_LAW_LJ || it.law > RDSIM_LAW_PIECEWISE_LINEAR)
@@ -807,6 +823,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       }
       if (rc > 0) R = std::max(R, rc);
       by_pair[it.type_a * MAXT + it.type_b].push_back(L);
+      by_pair_o[it.type_a * MAXT + it.type_b].push_back(it);
     }
     float R2 = 0.f;
     for (int a = 0; a < MAXT; a++)
@@ -815,6 +832,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         if (v.empty()) continue;
         int first = (int)laws.size() - sd.law0;
         if (first + (int)v.size() > 1023) return bail(fail(RDSIM_ERR_UNSUPPORTED, "too many pair laws"));
+        for (const rdsim_interaction& it : by_pair_o[a * MAXT + b]) olaws.push_back(it);
         for (auto& L : v) {
           laws.push_back(L);
           R2 = std::max(R2, L.rc2_hi);
@@ -984,6 +1002,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
           d.thr = (float)(tr.p0 - 0.1);
           int ti = (int)terms.size();
           terms.push_back(d);
+          oterms.push_back(tr);
           per_atom[tr.i].push_back(ti * 4 + 0);
           per_atom[tr.j].push_back(ti * 4 + 1);
           td.bondmask[tr.i] |= 1u << tr.j;
@@ -1103,6 +1122,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->tmpl_d, tmpls.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->terms_d, terms.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->atomterm_d, atomterm.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->olaws_d, olaws.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->owalls_d, owalls.size(), &B))) return bail(rc);
+  if ((rc = dalloc(&h->oterms_d, oterms.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->cell_count, (size_t)h->ncells, &B))) return bail(rc);
   // zero once; every rebuild leaves them zero for the next (k_scatter)
   if (cudaMemsetAsync(h->cell_count, 0, sizeof(int) * (size_t)h->ncells, h->stream) != cudaSuccess)
@@ -1160,6 +1182,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = up(h->tmpl_d, tmpls.data(), sizeof(TmplDev) * tmpls.size()))) return bail(rc);
   if ((rc = up(h->terms_d, terms.data(), sizeof(TermDev) * terms.size()))) return bail(rc);
   if ((rc = up(h->atomterm_d, atomterm.data(), sizeof(int) * atomterm.size()))) return bail(rc);
+  if ((rc = up(h->olaws_d, olaws.data(), sizeof(rdsim_interaction) * olaws.size()))) return bail(rc);
+  if ((rc = up(h->owalls_d, owalls.data(), sizeof(rdsim_interaction) * owalls.size()))) return bail(rc);
+  if ((rc = up(h->oterms_d, oterms.data(), sizeof(rdsim_term) * oterms.size()))) return bail(rc);
   if ((rc = up(h->sid, sid_h.data(), sizeof(int) * sid_h.size()))) return bail(rc);
   if ((rc = up(h->cl_d, cl.data(), sizeof(double) * cl.size()))) return bail(rc);
   if (cudaMemsetAsync(h->err, 0, sizeof(ErrDev), h->stream) != cudaSuccess)
@@ -1390,6 +1415,107 @@ int rdsim_get_cell_ids(rdsim_handle* h, int32_t sys, int32_t* cell_ids) {
   cudaStreamSynchronize(h->stream);
   cudaFree(buf);
   if (e1 != cudaSuccess) return fail(RDSIM_ERR_CUDA, cudaGetErrorString(e1));
+  return 0;
+}
+
+int rdsim_get_observables(rdsim_handle* h, int32_t sys, rdsim_observables* out) {
+  if (!h || !out || sys < 0 || sys >= h->nsys) return fail(RDSIM_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  const HostSys& q = h->hs[sys];
+  const int nb = std::max(1, (q.n + OBS_BLOCK - 1) / OBS_BLOCK);
+  if (nb > h->obs_cap) {
+    if (h->obs_part) cudaFree(h->obs_part);
+    h->obs_part = nullptr;
+    h->obs_cap = 0;
+    if (cudaMalloc(&h->obs_part, sizeof(double) * ((size_t)nb + 1) * OBS_NSUM) != cudaSuccess)
+      return fail(RDSIM_ERR_NOMEM, "observables scratch");
+    h->obs_cap = nb;
+  }
+  if (!h->obs_counts && cudaMalloc(&h->obs_counts, sizeof(unsigned long long) * (1 + MAXT)) != cudaSuccess)
+    return fail(RDSIM_ERR_NOMEM, "observables scratch");
+  ObsArgs o;
+  std::memset(&o, 0, sizeof o);
+  o.laws = h->olaws_d;
+  o.walls = h->owalls_d;
+  o.terms = h->oterms_d;
+  o.part = h->obs_part;
+  o.sums = h->obs_part + (size_t)nb * OBS_NSUM;
+  o.counts = h->obs_counts;
+  o.sys = sys;
+  o.tpp = h->ltpp;
+  o.nblocks = nb;
+  CK(cudaMemsetAsync(h->obs_counts, 0, sizeof(unsigned long long) * (1 + MAXT), h->stream));
+  Args a = make_args(h);
+  {
+    ProfScope ps(h, 4, 2);
+    if (h->D == 2) k_observe<2><<<nb, OBS_BLOCK, 0, h->stream>>>(a, o);
+    else if (h->D == 3) k_observe<3><<<nb, OBS_BLOCK, 0, h->stream>>>(a, o);
+    else k_observe<1><<<nb, OBS_BLOCK, 0, h->stream>>>(a, o);
+    k_observe_sum<<<1, OBS_BLOCK, 0, h->stream>>>(o);
+  }
+  CK(cudaGetLastError());
+  double sums[OBS_NSUM];
+  unsigned long long counts[1 + MAXT];
+  CK(cudaMemcpyAsync(sums, o.sums, sizeof sums, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(counts, h->obs_counts, sizeof counts, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  std::memset(out, 0, sizeof *out);
+  out->pair_energy = sums[0];
+  out->wall_energy = sums[1];
+  out->bond_energy = sums[2];
+  out->angle_energy = sums[3];
+  out->virial = sums[4];
+  out->min_distance = sums[5];
+  out->n_pairs = (int64_t)counts[0];
+  out->n_particles = q.n;
+  for (int t = 0; t < MAXT; t++) out->type_counts[t] = (int64_t)counts[1 + t];
+  return 0;
+}
+
+int rdsim_get_rdf(rdsim_handle* h, int32_t sys, int32_t type_a, int32_t type_b, double r_max,
+                  int32_t n_bins, int32_t flags, int64_t* counts) {
+  if (!h || !counts || sys < 0 || sys >= h->nsys) return fail(RDSIM_ERR_ARG, "bad argument");
+  if (n_bins < 1 || n_bins > RDF_MAX_BINS) return fail(RDSIM_ERR_ARG, "n_bins must be in [1, 8192]");
+  if (!(r_max > 0) || !std::isfinite(r_max)) return fail(RDSIM_ERR_ARG, "r_max must be positive");
+  if (type_a >= MAXT || type_b >= MAXT) return fail(RDSIM_ERR_ARG, "type out of range");
+  const HostSys& q = h->hs[sys];
+  const SysDev& sd = h->sys_h[sys];
+  RdfArgs o;
+  std::memset(&o, 0, sizeof o);
+  double maxu = 0;
+  for (int k = 0; k < h->D; k++) {
+    if (((sd.periodic >> k) & 1) && r_max > 0.5 * q.L[k])
+      return fail(RDSIM_ERR_ARG, "r_max exceeds half of a periodic box length");
+    maxu = std::max(maxu, (double)sd.unit_hi[k]);
+    // pairs closer than r_max now were within r_max + 2 delta at the rebuild
+    const double cell = q.L[k] / sd.nc[k];
+    const double reach = r_max + 2.0 * (double)sd.delta * 1.01 + 8.0 * maxu;
+    o.h[k] = (int)std::min<double>(sd.nc[k], std::floor(reach / cell) + 1.0);
+  }
+  CK(cudaSetDevice(h->device));
+  if (!h->rdf_counts && cudaMalloc(&h->rdf_counts, sizeof(unsigned long long) * RDF_MAX_BINS) != cudaSuccess)
+    return fail(RDSIM_ERR_NOMEM, "histogram scratch");
+  o.counts = h->rdf_counts;
+  o.r_max = r_max;
+  o.width = r_max / n_bins;
+  o.r2_hi = (float)(r_max * r_max) + guard2(r_max, maxu);
+  o.sys = sys;
+  o.type_a = type_a;
+  o.type_b = type_b;
+  o.nbins = n_bins;
+  o.flags = flags;
+  CK(cudaMemsetAsync(h->rdf_counts, 0, sizeof(unsigned long long) * n_bins, h->stream));
+  Args a = make_args(h);
+  const unsigned nb = (unsigned)std::max(1, (q.n + OBS_BLOCK - 1) / OBS_BLOCK);
+  {
+    ProfScope ps(h, 4, 1);
+    if (h->D == 2) k_rdf<2><<<nb, OBS_BLOCK, 0, h->stream>>>(a, o);
+    else if (h->D == 3) k_rdf<3><<<nb, OBS_BLOCK, 0, h->stream>>>(a, o);
+    else k_rdf<1><<<nb, OBS_BLOCK, 0, h->stream>>>(a, o);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(counts, h->rdf_counts, sizeof(int64_t) * n_bins, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return 0;
 }
 

@@ -23,6 +23,7 @@ EXPORTS = [
     "rdsim_get_step", "rdsim_set_step", "rdsim_set_trajectory", "rdsim_get_trajectory",
     "rdsim_get_error", "rdsim_get_stream", "rdsim_get_info", "rdsim_last_error",
     "rdsim_set_profiling", "rdsim_get_profile", "rdsim_get_pairs_static",
+    "rdsim_get_observables", "rdsim_get_rdf",
 ]
 
 
@@ -56,6 +57,9 @@ def load_library(path=None):
     L.rdsim_get_pairs.argtypes = [vp, C.c_int32, ip, C.c_int64, C.POINTER(C.c_int64)]
     L.rdsim_get_pairs_static.argtypes = [vp, C.c_int32, ip, C.c_int64, C.POINTER(C.c_int64)]
     L.rdsim_get_cell_ids.argtypes = [vp, C.c_int32, ip]
+    L.rdsim_get_observables.argtypes = [vp, C.c_int32, C.POINTER(abi.Observables)]
+    L.rdsim_get_rdf.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                C.c_int32, C.POINTER(C.c_int64)]
     L.rdsim_get_step.argtypes = [vp, C.POINTER(C.c_int64)]
     L.rdsim_set_step.argtypes = [vp, C.c_int64]
     L.rdsim_set_trajectory.argtypes = [vp, C.c_int32, C.c_int32]
@@ -77,6 +81,22 @@ def _check(rc):
         if rc == abi.ERR_OUT_OF_BOUNDS:
             raise EngineError(rc, msg)
         raise EngineError(rc, msg)
+
+
+def rdf_normalise(counts, r_max, n_dim, volume, n_pairs):
+    """g(r) from a pair histogram: counts / (n_pairs * shell volume / volume).
+    Returns (bin centres, g, counts)."""
+    counts = np.asarray(counts)
+    edges = np.linspace(0.0, float(r_max), counts.size + 1)
+    if n_dim == 1:
+        shell = 2.0 * np.diff(edges)
+    elif n_dim == 2:
+        shell = np.pi * np.diff(edges ** 2)
+    else:
+        shell = 4.0 / 3.0 * np.pi * np.diff(edges ** 3)
+    ideal = n_pairs * shell / volume
+    g = np.where(ideal > 0, counts / np.where(ideal > 0, ideal, 1.0), 0.0)
+    return 0.5 * (edges[1:] + edges[:-1]), g, counts
 
 
 class Engine:
@@ -175,6 +195,49 @@ class Engine:
         c = np.empty((n, self.D), dtype=np.int32)
         _check(self.lib.rdsim_get_cell_ids(self.h, sys, abi.iptr(c)))
         return c
+
+    # ---- observables (float64 device reductions) ------------------------
+    def observables(self, sys=0):
+        """Energies, virial, minimum partner distance, pair and type counts
+        of system ``sys`` at the current state (see ``rdsim_get_observables``)."""
+        o = abi.Observables()
+        _check(self.lib.rdsim_get_observables(self.h, int(sys), C.byref(o)))
+        return o.as_dict()
+
+    def rdf_counts(self, r_max, n_bins=100, type_a=-1, type_b=-1, sys=0,
+                   other_molecules=False):
+        """Histogram of pair distances below ``r_max`` (``n_bins`` bins) over
+        unordered pairs of types {type_a, type_b} (-1: any)."""
+        counts = np.zeros(int(n_bins), dtype=np.int64)
+        flags = abi.RDF_OTHER_MOLECULES if other_molecules else 0
+        _check(self.lib.rdsim_get_rdf(self.h, int(sys), int(type_a), int(type_b),
+                                      float(r_max), int(n_bins), flags,
+                                      counts.ctypes.data_as(C.POINTER(C.c_int64))))
+        return counts
+
+    def rdf(self, r_max, n_bins=100, type_a=-1, type_b=-1, sys=0, other_molecules=False):
+        """Radial distribution function g(r) at the bin centres: the pair
+        histogram divided by the count an ideal gas of the same densities
+        would give in each shell (no correction for reflecting walls).
+        Returns (r, g, counts)."""
+        counts = self.rdf_counts(r_max, n_bins, type_a, type_b, sys, other_molecules)
+        sd = self.systems[sys]
+        m = sd.model
+        D = m.N_dim
+        vol = float(np.prod(np.asarray(m.L, dtype=float)[:D]))
+        t = np.asarray(self.state()[1][self.offsets[sys]:self.offsets[sys + 1]])
+        n = t.size
+        if type_a < 0 and type_b < 0:
+            pairs = 0.5 * n * (n - 1)
+        elif type_a < 0 or type_b < 0:  # pairs with at least one particle of the type
+            nt = int((t == max(type_a, type_b)).sum())
+            pairs = 0.5 * nt * (nt - 1) + nt * (n - nt)
+        elif type_a == type_b:
+            nt = int((t == type_a).sum())
+            pairs = 0.5 * nt * (nt - 1)
+        else:
+            pairs = float((t == type_a).sum()) * float((t == type_b).sum())
+        return rdf_normalise(counts, r_max, D, vol, pairs)
 
     @property
     def step_index(self):

@@ -52,6 +52,7 @@ def test_struct_sizes_match_header(lib):
     assert ctypes.sizeof(abi.Term) == 4 * 4 + 2 * 8
     assert ctypes.sizeof(abi.Template) == 16
     assert abi.System.seed.offset % 8 == 0
+    assert ctypes.sizeof(abi.Observables) == 6 * 8 + 2 * 8 + abi.MAX_TYPES * 8
 
 
 def test_last_error_is_callable_without_gpu(lib):

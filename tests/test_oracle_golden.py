@@ -68,3 +68,72 @@ def test_cell_geometry_matches_reference():
             while m.L[k] / float(l + 1) >= m.rs / ratio:
                 l += 1
             assert m.L[k] / float(l) == fx["init_cell_length"][k]
+
+
+def _total_energy(o):
+    ob = o.observables()
+    return ob["pair_energy"] + ob["wall_energy"] + ob["bond_energy"] + ob["angle_energy"]
+
+
+def _pi_expansion_quirk(sd):
+    """Particles of molecules with an angle term whose theta0 is not pi while
+    the system's theta0 == pi flag is set: the reference then evaluates that
+    term with the expansion about pi (pyrdsim.pyx:1350-1401), a force that is
+    not the gradient of k (theta - theta0)^2 / 2."""
+    from pyrdsim_gb300 import abi
+    skip = np.zeros(sd.n_particles, bool)
+    if sd.struct.angle_is_pi <= 0:
+        return skip
+    ids = set()
+    for q in range(sd.struct.n_templates):
+        T = sd.tmpl[q]
+        for e in range(T.first_term, T.first_term + T.n_terms):
+            tm = sd.terms[e]
+            if tm.kind == abi.TERM_ANGLE and abs(tm.p0 - np.pi) > 1e-12:
+                ids.add(T.molecule_id)
+    return np.isin(sd.molecule_ids[:, 2], sorted(ids))
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_observable_potentials_integrate_the_force_laws(name):
+    """The potentials of the observables are those whose gradients are the
+    reference's drift: -dU/dx by central differences equals the oracle's
+    drift (pinned to the reference above) for every particle and dimension."""
+    fx = load_fixture(name)
+    sd = system_from_deck(deck_dict(fx), int(fx["seed"]))
+    o = Oracle(sd, history_quirk=False)
+    x0, t0 = o.state()
+    a = o.drift()
+    h = 1e-6
+    fd = np.zeros_like(a)
+    for i in range(sd.n_particles):
+        for k in range(sd.model.N_dim):
+            x = x0.copy()
+            x[i, k] += h
+            o.set_state(x, t0)
+            ep = _total_energy(o)
+            x[i, k] -= 2 * h
+            o.set_state(x, t0)
+            em = _total_energy(o)
+            fd[i, k] = -(ep - em) / (2 * h)
+    keep = ~_pi_expansion_quirk(sd)
+    assert keep.sum() >= sd.n_particles // 3
+    scale = max(np.abs(a).max(), 1.0)
+    err = np.abs(fd - a)[keep].max()
+    assert err <= 1e-5 * scale, err / scale
+
+
+def test_rdf_oracle_counts_every_pair_once():
+    fx = load_fixture("lj_periodic")
+    sd = system_from_deck(deck_dict(fx), int(fx["seed"]))
+    o = Oracle(sd, history_quirk=False)
+    x, _ = o.state()
+    L = np.asarray(sd.model.L)
+    r_max = 0.5 * L.min()
+    c = o.rdf_counts(r_max, 50)
+    d = x[:, None, :] - x[None, :, :]
+    d -= L * np.round(d / L)
+    r = np.sqrt((d ** 2).sum(-1))[np.triu_indices(sd.n_particles, 1)]
+    ref, _ = np.histogram(r[r < r_max], bins=50, range=(0.0, r_max))
+    assert c.sum() == (r < r_max).sum()
+    assert np.abs(c - ref).sum() <= 2  # numpy's bin edges round differently
