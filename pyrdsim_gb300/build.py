@@ -1,7 +1,9 @@
 """Builds the CUDA engine ``pyrdsim_gb300/_lib/librdsim.so`` for sm_103a.
 
-One translation unit (``csrc/engine.cu``) compiled by nvcc into a plain
-shared library with a C ABI (``include/rdsim.h``); no PyTorch headers.
+Two translation units (``csrc/engine.cu``: the step engine and observables;
+``csrc/adjoint.cu``: the differentiable reaction-free steps) compiled by nvcc
+in parallel and linked into one plain shared library with a C ABI
+(``include/rdsim.h``, ``include/rdsim_adjoint.h``); no PyTorch headers.
 """
 from __future__ import annotations
 
@@ -25,8 +27,11 @@ def _nvcc():
     raise RuntimeError("nvcc not found")
 
 
+UNITS = ["engine.cu", "adjoint.cu"]
+
+
 def sources():
-    out = [os.path.join(INCLUDE, "rdsim.h")]
+    out = [os.path.join(INCLUDE, f) for f in sorted(os.listdir(INCLUDE)) if f.endswith(".h")]
     for f in sorted(os.listdir(CSRC)):
         if f.endswith((".cu", ".cuh", ".h")):
             out.append(os.path.join(CSRC, f))
@@ -38,11 +43,19 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if not force and os.path.exists(LIB):
         if os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in sources()):
             return LIB
-    cmd = [_nvcc(), "-std=c++17", "-O3", "-lineinfo", "-shared", "-Xcompiler", "-fPIC",
-           *ARCH, "-o", LIB + ".tmp", os.path.join(CSRC, "engine.cu")]
+    nvcc = _nvcc()
+    flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", *ARCH]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.check_call(cmd)
+        flags.insert(0, "-Xptxas=-v")
+    objs, procs = [], []
+    for u in UNITS:
+        obj = os.path.join(LIBDIR, u.replace(".cu", ".o"))
+        objs.append(obj)
+        procs.append(subprocess.Popen([nvcc, *flags, "-c", os.path.join(CSRC, u), "-o", obj]))
+    codes = [p.wait() for p in procs]
+    if any(codes):
+        raise subprocess.CalledProcessError(max(codes), "nvcc")
+    subprocess.check_call([nvcc, "-shared", *ARCH, "-o", LIB + ".tmp", *objs])
     os.replace(LIB + ".tmp", LIB)
     return LIB
 

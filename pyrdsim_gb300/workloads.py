@@ -189,3 +189,44 @@ def ensemble(n_systems=512, seed=4, dt=1e-4, n_min=256, n_max=16384):
         mol, first = _single_atoms(n)
         out.append(model.SystemData(m, x, types, mol, first))
     return out
+
+
+def mixed_lj_yukawa(n=16384, rho=0.5, seed=5, dt=1e-4):
+    """Reaction-free mixture for gradients: 2D periodic box at number density
+    ``rho``, species drawn 50/50, jittered-lattice start.  Lennard-Jones
+    (epsilon = 1, sigma = 1, cut 2.5) between all pairs; Yukawa U = A
+    exp(-kappa r) / r (A = 5, kappa = 2, cut 3) between species-1 pairs.
+    ``theta`` = (epsilon, sigma, A, kappa); cutoffs stay fixed when theta
+    changes."""
+    rng = np.random.default_rng(seed)
+    L = float(np.sqrt(n / rho))
+    x = jittered_lattice(n, [L, L], rng)
+    types = (rng.random(n) < 0.5).astype(np.int32)
+    return {"n_dim": 2, "L": [L, L], "dt": dt, "mobility": np.array([1.0, 1.0]),
+            "types": types, "x0": x, "theta": np.array([1.0, 1.0, 5.0, 2.0]),
+            "pairs": [(0, 0), (0, 1), (1, 1)], "rc_lj": 2.5, "rc_yukawa": 3.0}
+
+
+def mixed_lj_yukawa_params(theta):
+    """(u0, r0) of the four laws of :func:`mixed_lj_yukawa` from theta =
+    (epsilon, sigma, A, kappa): three LJ laws with u0 = epsilon, r0 = 2^(1/6)
+    sigma, then the Yukawa law with u0 = A, r0 = 1 / kappa.  Works on numpy
+    arrays and on torch tensors (differentiably)."""
+    eps, sig, A, kap = theta[0], theta[1], theta[2], theta[3]
+    rows = [[eps, WCA_R0 * sig]] * 3 + [[A, 1.0 / kap]]
+    try:
+        import torch
+        if isinstance(theta, torch.Tensor):
+            return torch.stack([torch.stack(r) for r in rows])
+    except ImportError:
+        pass
+    return np.array(rows, dtype=np.float64)
+
+
+def mixed_lj_yukawa_laws(w):
+    """The four laws (abi.Interaction) of :func:`mixed_lj_yukawa` at its theta."""
+    from .adjoint import law
+    p = mixed_lj_yukawa_params(w["theta"])
+    out = [law("lj", pr, p[q, 0], p[q, 1], w["rc_lj"]) for q, pr in enumerate(w["pairs"])]
+    out.append(law("yukawa", (1, 1), p[3, 0], p[3, 1], w["rc_yukawa"]))
+    return out

@@ -9,11 +9,16 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
-    with open(os.path.join(ROOT, "include", "rdsim.h")) as f:
-        text = f.read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(rdsim_[a-z_]+)\s*\(", text)))
+def declared_functions(header=None):
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for h in sorted(os.listdir(inc)) if header is None else [header]:
+        if not h.endswith(".h"):
+            continue
+        with open(os.path.join(inc, h)) as f:
+            text = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+        names |= set(re.findall(r"\b(rdsim_[a-z_]+)\s*\(", text))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")
@@ -39,8 +44,9 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_binding_declares_every_export():
-    from pyrdsim_gb300 import engine
-    assert sorted(engine.EXPORTS) == declared_functions()
+    from pyrdsim_gb300 import adjoint, engine
+    assert sorted(engine.EXPORTS) == declared_functions("rdsim.h")
+    assert sorted(adjoint.EXPORTS) == declared_functions("rdsim_adjoint.h")
 
 
 def test_struct_sizes_match_header(lib):
@@ -53,6 +59,9 @@ def test_struct_sizes_match_header(lib):
     assert ctypes.sizeof(abi.Template) == 16
     assert abi.System.seed.offset % 8 == 0
     assert ctypes.sizeof(abi.Observables) == 6 * 8 + 2 * 8 + abi.MAX_TYPES * 8
+    from pyrdsim_gb300.adjoint import AdjointSystemStruct
+    assert AdjointSystemStruct.mobility.offset == 16 + 3 * 8 + 8
+    assert ctypes.sizeof(AdjointSystemStruct) == 16 + 4 * 8 + 3 * 8 + 8
 
 
 def test_last_error_is_callable_without_gpu(lib):

@@ -1,0 +1,133 @@
+"""GPU adjoint of the reaction-free steps (include/rdsim_adjoint.h) against
+the dense float64 autograd reference (tests/dense_reference.py, itself
+pinned by finite differences) and against finite differences of the GPU
+forward pass.
+
+Bars: loss within 1e-12 relative of the dense reference; dL/dx0 within 1e-9
+(norm-wise) and dL/dtheta within 1e-9 relative (both float64, summed in
+other orders); finite differences (h = 1e-4 relative for the parameters,
+1e-5 along a unit direction of x0) within 1e-4 / 2e-3 relative (the loss
+jumps where a pair crosses a cutoff, which finite differences see).
+"""
+import numpy as np
+import pytest
+
+from dense_reference import LAW_LJ, LAW_YUKAWA, dense_loss
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _setup(n=1024, steps=40, K=20, E=7, seed=5):
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.adjoint import Adjoint
+    w = workloads.mixed_lj_yukawa(n=n, seed=seed)
+    adj = Adjoint(2, w["L"], w["dt"], w["mobility"], w["types"], workloads.mixed_lj_yukawa_laws(w),
+                  loss_steps=K, checkpoint_every=E)
+    rng = np.random.default_rng(seed + 1)
+    xi = torch.tensor(rng.standard_normal((steps, n, 2)), dtype=torch.float64, device="cuda")
+    x0 = torch.tensor(w["x0"], dtype=torch.float64, device="cuda")
+    return w, adj, xi, x0, K
+
+
+def _dense_laws(w):
+    laws = [(LAW_LJ, 6, a, b, w["rc_lj"]) for (a, b) in w["pairs"]]
+    laws.append((LAW_YUKAWA, 0, 1, 1, w["rc_yukawa"]))
+    return laws
+
+
+def test_adjoint_matches_dense_autograd():
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.adjoint import trajectory_loss
+    w, adj, xi, x0, K = _setup()
+    theta = torch.tensor(w["theta"], dtype=torch.float64, requires_grad=True)
+    x0g = x0.clone().requires_grad_(True)
+    loss = trajectory_loss(x0g, workloads.mixed_lj_yukawa_params(theta), xi, adj)
+    loss.backward()
+    theta_d = torch.tensor(w["theta"], dtype=torch.float64, device="cuda", requires_grad=True)
+    x0d = x0.clone().requires_grad_(True)
+    ref = dense_loss(x0d, workloads.mixed_lj_yukawa_params(theta_d), xi, w["types"],
+                     _dense_laws(w), w["L"], w["dt"], w["mobility"], K)
+    ref.backward()
+    lv, rv = loss.item(), ref.item()
+    assert abs(lv - rv) <= 1e-12 * abs(rv), (lv, rv)
+    gx, rx = x0g.grad, x0d.grad
+    assert float((gx - rx).norm() / rx.norm()) <= 1e-9
+    gt, rt = theta.grad.numpy(), theta_d.grad.cpu().numpy()
+    np.testing.assert_allclose(gt, rt, rtol=1e-9, atol=0)
+
+
+def test_adjoint_matches_finite_differences():
+    from pyrdsim_gb300 import workloads
+    w, adj, xi, x0, K = _setup()
+    theta = np.array(w["theta"], dtype=np.float64)
+    adj.forward(x0, workloads.mixed_lj_yukawa_params(theta), xi)
+    gx, gp = adj.backward()
+    gp = gp.numpy()
+    # chain rule of the parameter map: theta = (eps, sigma, A, kappa)
+    r0s = 2.0 ** (1.0 / 6.0)
+    g_theta = np.array([gp[:3, 0].sum(), r0s * gp[:3, 1].sum(), gp[3, 0],
+                        -gp[3, 1] / theta[3] ** 2])
+    for q in range(4):
+        h = 1e-4 * abs(theta[q])
+        tp, tm = theta.copy(), theta.copy()
+        tp[q] += h
+        tm[q] -= h
+        lp, _ = adj.forward(x0, workloads.mixed_lj_yukawa_params(tp), xi)
+        lm, _ = adj.forward(x0, workloads.mixed_lj_yukawa_params(tm), xi)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g_theta[q]) <= 1e-4 * abs(g_theta[q]), (q, fd, g_theta[q])
+    rng = np.random.default_rng(9)
+    u = torch.tensor(rng.standard_normal(tuple(x0.shape)), dtype=torch.float64, device="cuda")
+    u /= u.norm()
+    h = 1e-5
+    p0 = workloads.mixed_lj_yukawa_params(theta)
+    lp, _ = adj.forward(x0 + h * u, p0, xi)
+    lm, _ = adj.forward(x0 - h * u, p0, xi)
+    fd = (lp - lm) / (2 * h)
+    g = float((gx * u).sum())
+    assert abs(fd - g) <= 2e-3 * abs(g), (fd, g)
+
+
+def test_checkpoint_interval_does_not_change_results():
+    from pyrdsim_gb300 import workloads
+    out = []
+    for E in (1, 7, 64):
+        w, adj, xi, x0, K = _setup(n=1024, steps=30, K=30, E=E)
+        loss, xT = adj.forward(x0, workloads.mixed_lj_yukawa_params(w["theta"]), xi)
+        gx, gp = adj.backward()
+        out.append((loss, xT.cpu().numpy(), gx.cpu().numpy(), gp.numpy()))
+    for o in out[1:]:
+        assert o[0] == out[0][0]
+        for a, b in zip(o[1:], out[0][1:]):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_backward_scales_and_guards_generations():
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.adjoint import trajectory_loss
+    w, adj, xi, x0, K = _setup(n=1024, steps=10, K=5)
+    p = workloads.mixed_lj_yukawa_params(w["theta"])
+    adj.forward(x0, p, xi)
+    g1, p1 = adj.backward()
+    g2, p2 = adj.backward(2.5)
+    torch.testing.assert_close(g2, 2.5 * g1, rtol=1e-15, atol=0)
+    np.testing.assert_allclose(p2.numpy(), 2.5 * p1.numpy(), rtol=1e-15)
+    x0g = x0.clone().requires_grad_(True)
+    loss = trajectory_loss(x0g, torch.tensor(p), xi, adj)
+    adj.forward(x0, p, xi)  # a second forward pass on the handle
+    with pytest.raises(RuntimeError):
+        loss.backward()
+
+
+def test_adjoint_rejects_bad_systems():
+    from pyrdsim_gb300.adjoint import Adjoint, law
+    from pyrdsim_gb300.engine import EngineError
+    with pytest.raises(EngineError):  # box below twice the cutoff
+        Adjoint(2, [4.0, 4.0], 1e-4, [1.0], np.zeros(8, np.int32),
+                [law("lj", (0, 0), 1.0, 1.12, 2.5)], loss_steps=1)
+    with pytest.raises(EngineError):  # unsupported law
+        bad = law("lj", (0, 0), 1.0, 1.12, 2.5)
+        bad.law = 2
+        Adjoint(2, [10.0, 10.0], 1e-4, [1.0], np.zeros(8, np.int32), [bad], loss_steps=1)
