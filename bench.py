@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--segment", type=int, default=SEGMENT)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true")
     return p.parse_args()
 
 
@@ -222,6 +223,42 @@ def ensemble_comparison(local, steps=100, n_systems=512):
                         "kT U[0.5, 2], LJ or Yukawa, half with two-state reactions"}
 
 
+def adjoint_timing(local, n=16384, steps=1000, loss_steps=500, every=32, reps=2):
+    """Loss and gradients of the reaction-free mixture (LJ + Yukawa, N =
+    16,384, density 0.5, 1,000 steps, loss over the last 500 states,
+    checkpoints every 32 steps): wall time of the forward and the backward
+    call (each returns after synchronising its stream), best of ``reps``."""
+    import numpy as np
+    import torch
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.adjoint import Adjoint
+    w = workloads.mixed_lj_yukawa(n=n)
+    adj = Adjoint(2, w["L"], w["dt"], w["mobility"], w["types"],
+                  workloads.mixed_lj_yukawa_laws(w), loss_steps=loss_steps,
+                  checkpoint_every=every, device=local)
+    gen = torch.Generator(device=f"cuda:{local}").manual_seed(5)
+    xi = torch.randn((steps, n, 2), dtype=torch.float64, device=f"cuda:{local}", generator=gen)
+    x0 = torch.tensor(w["x0"], dtype=torch.float64, device=f"cuda:{local}")
+    p = workloads.mixed_lj_yukawa_params(w["theta"])
+    best_f = best_b = float("inf")
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss, _ = adj.forward(x0, p, xi)
+        t1 = time.perf_counter()
+        gx, gp = adj.backward()
+        t2 = time.perf_counter()
+        best_f, best_b = min(best_f, t1 - t0), min(best_b, t2 - t1)
+    adj.close()
+    return {"workload": "2D LJ+Yukawa mixture, N=16384, density 0.5, 1000 steps, loss over the "
+                        "last 500 states, checkpoints every 32 steps, float64",
+            "forward_ms": 1e3 * best_f, "backward_ms": 1e3 * best_b,
+            "particle_steps_per_s_forward": n * steps / best_f,
+            "particle_steps_per_s_forward_backward": n * steps / (best_f + best_b),
+            "loss": loss, "grad_params_norm": float(np.linalg.norm(gp.numpy())),
+            "grad_x0_norm": float(gx.norm())}
+
+
 def run_ours(args, rank, ws, local):
     import numpy as np
     import torch
@@ -326,6 +363,11 @@ def run_ours(args, rank, ws, local):
             out["ensemble"] = ensemble_comparison(local)
         except Exception as exc:
             out["ensemble"] = {"unavailable": str(exc)[:200]}
+    if rank == 0 and ws == 1 and not args.no_adjoint:
+        try:
+            out["adjoint"] = adjoint_timing(local)
+        except Exception as exc:
+            out["adjoint"] = {"unavailable": str(exc)[:200]}
     if rank == 0:
         print(json.dumps(out))
 

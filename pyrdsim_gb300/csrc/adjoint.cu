@@ -3,9 +3,12 @@
 // pair-law parameters), for include/rdsim_adjoint.h.
 //
 // Every state is binned into cells (counting sort, then each cell's members
-// in index order, so all sums run in a fixed order and results are
-// deterministic); one thread per particle then walks the 3^D cells around
-// its own.  Forward (k_adj_step): pair drift of pyrdsim.pyx:1941-2067 for
+// in index order) and gets a neighbour list: the particles of the 3^D
+// cells around each particle that pass a float32 distance screen, in a fixed
+// order, so all sums run in a fixed order and results are deterministic.
+// The float64 kernels walk the lists with four lanes per particle: float64
+// issue is scarce on this GPU (1/64 of float32), and a compact list keeps
+// the lanes of a warp busy with pairs inside the cutoff.  Forward (k_adj_step): pair drift of pyrdsim.pyx:1941-2067 for
 // Lennard-Jones and Yukawa laws (pyrdsim.pyx:1068-1130), the loss terms of
 // the state, and the Euler-Maruyama update with injected noise and periodic
 // wrap (pyrdsim.pyx:2225-2292).  Backward (k_adj_back): for state x_n and
@@ -50,7 +53,7 @@ int fail(int code, const std::string& m) {
 
 struct Law {
   int law, n;
-  double u0, r0, rc;
+  double u0, r0, rc, ir0;       // ir0 = 1 / r0
   double Uc, dUc_du0, dUc_dr0;  // energy at rc and its parameter derivatives
 };
 
@@ -58,6 +61,8 @@ struct AdjArgs {
   int N, D, nlaws;
   int nc[3], ncell;
   double L[3], cellinv[3];
+  float Lf[3], Linvf[3];
+  float cut2f;                  // float32 screen: above the largest rc^2
   double c[MAXT], s[MAXT];      // dt D and sqrt(2 dt D) per type
   double wU, wW;                // loss weights 1/K and 1/(K d V)
   unsigned char lawmask[MAXT * MAXT];  // bit l: law l applies to (ti, tj)
@@ -65,9 +70,10 @@ struct AdjArgs {
 };
 
 enum { F_STEP = 1, F_LOSS = 2 };
+constexpr int TPP = 4;  // lanes per particle in the pair kernels
 
-// Pair terms of one law at distance r < rc: U (unshifted), f = dU/dr,
-// fp = d2U/dr2, and the derivatives of U and f by (u0, r0).
+// Pair terms of one law at distance r < rc (ir = 1 / r): U (unshifted),
+// f = dU/dr, fp = d2U/dr2, and the derivatives of U and f by (u0, r0).
 struct PairEval {
   double U, f, fp, dU[2], df[2];
 };
@@ -83,29 +89,31 @@ __host__ __device__ inline double lj_power(double q, int n) {
   return s;
 }
 
-__host__ __device__ inline PairEval eval_law(const Law& w, double r) {
+__host__ __device__ inline PairEval eval_law(const Law& w, double r, double ir) {
   PairEval p;
   if (w.law == RDSIM_LAW_LJ) {
     // U = u0 (s^2 - 2 s), s = (r0/r)^n; f = -2 n u0 s (s - 1) / r
     const double n = (double)w.n;
-    const double s = lj_power(w.r0 / r, w.n);
+    const double s = lj_power(w.r0 * ir, w.n);
+    const double t = 2.0 * n * s * ir;
     p.U = w.u0 * s * (s - 2.0);
-    p.f = -2.0 * n * w.u0 * s * (s - 1.0) / r;
-    p.fp = 2.0 * n * w.u0 * s * ((2.0 * n + 1.0) * s - (n + 1.0)) / (r * r);
+    p.f = -w.u0 * t * (s - 1.0);
+    p.fp = w.u0 * t * ((2.0 * n + 1.0) * s - (n + 1.0)) * ir;
     p.dU[0] = s * (s - 2.0);
-    p.df[0] = -2.0 * n * s * (s - 1.0) / r;
+    p.df[0] = -t * (s - 1.0);
     // ds/dr0 = n s / r0
-    p.dU[1] = 2.0 * n * w.u0 * s * (s - 1.0) / w.r0;
-    p.df[1] = -2.0 * n * n * w.u0 * s * (2.0 * s - 1.0) / (r * w.r0);
+    p.dU[1] = 2.0 * n * w.u0 * s * (s - 1.0) * w.ir0;
+    p.df[1] = -w.u0 * t * n * (2.0 * s - 1.0) * w.ir0;
   } else {
     // Yukawa: U = u0 e / r, e = exp(-r / r0)
-    const double e = exp(-r / w.r0);
-    const double ir = 1.0 / r, ir0 = 1.0 / w.r0;
+    const double e = exp(-r * w.ir0);
+    const double ir0 = w.ir0;
+    const double h = ir * ir0 + ir * ir;
     p.U = w.u0 * e * ir;
-    p.f = -w.u0 * e * (ir * ir0 + ir * ir);
-    p.fp = w.u0 * e * (ir * ir0 * ir0 + 2.0 * ir * ir * ir0 + 2.0 * ir * ir * ir);
+    p.f = -w.u0 * e * h;
+    p.fp = w.u0 * e * ir * (ir0 * ir0 + 2.0 * ir * ir0 + 2.0 * ir * ir);
     p.dU[0] = e * ir;
-    p.df[0] = -e * (ir * ir0 + ir * ir);
+    p.df[0] = -e * h;
     p.dU[1] = w.u0 * e * ir0 * ir0;
     p.df[1] = -w.u0 * e * ir0 * ir0 * ir0;
   }
@@ -124,7 +132,7 @@ __global__ void k_bin(AdjArgs g, const double* __restrict__ x, int* __restrict__
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.N) return;
   int c = 0, mult = 1;
-  #pragma unroll
+#pragma unroll
   for (int k = 0; k < D; k++) {
     c += cell_of(g, k, x[(size_t)i * D + k]) * mult;
     mult *= g.nc[k];
@@ -173,7 +181,7 @@ __global__ void k_fill(AdjArgs g, const double* __restrict__ x, int* __restrict_
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.N) return;
   int c = 0, mult = 1;
-  #pragma unroll
+#pragma unroll
   for (int k = 0; k < D; k++) {
     c += cell_of(g, k, x[(size_t)i * D + k]) * mult;
     mult *= g.nc[k];
@@ -181,9 +189,13 @@ __global__ void k_fill(AdjArgs g, const double* __restrict__ x, int* __restrict_
   idx[atomicAdd(cursor + c, 1)] = i;
 }
 
-// Members of each cell in index order; clears the counts for the next build.
-__global__ void k_cell_sort(int ncell, const int* __restrict__ start, int* __restrict__ idx,
-                            int* __restrict__ count) {
+// Members of each cell in index order, and their float32 positions in the
+// same order (the screen of the pair kernels); clears the counts for the
+// next build.
+template <int D>
+__global__ void k_cell_sort(int ncell, const double* __restrict__ x,
+                            const int* __restrict__ start, int* __restrict__ idx,
+                            float* __restrict__ xs, int* __restrict__ count) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
   const int b = start[c], e = start[c + 1];
@@ -196,96 +208,161 @@ __global__ void k_cell_sort(int ncell, const int* __restrict__ start, int* __res
     }
     idx[q + 1] = v;
   }
+  for (int p = b; p < e; p++) {
+    const int j = idx[p];
+#pragma unroll
+    for (int k = 0; k < D; k++) xs[(size_t)p * D + k] = (float)x[(size_t)j * D + k];
+  }
   count[c] = 0;
 }
 
-// Visit every particle j != i in the 3^D cells around particle i (each cell
-// once), with the minimum-image vector d = x_j - x_i.
-template <int D, class Fn>
-__device__ inline void for_neighbours(const AdjArgs& g, const double* __restrict__ x,
-                                      const int* __restrict__ start, const int* __restrict__ idx,
-                                      int i, const double* xi, Fn&& fn) {
-  int c[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-  #pragma unroll
-  for (int k = 0; k < D; k++) {
-    c[k] = cell_of(g, k, xi[k]);
-    if (g.nc[k] >= 3) {
-      lo[k] = c[k] - 1;
-      hi[k] = c[k] + 1;
-    } else {
-      lo[k] = 0;
-      hi[k] = g.nc[k] - 1;
-    }
-  }
-  for (int cz = lo[2]; cz <= hi[2]; cz++)
-    for (int cy = lo[1]; cy <= hi[1]; cy++)
-      for (int cx = lo[0]; cx <= hi[0]; cx++) {
-        const int cc[3] = {cx, cy, cz};
-        int cell = 0, mult = 1;
-        #pragma unroll
-        for (int k = 0; k < D; k++) {
-          int ck = cc[k];
-          if (ck < 0) ck += g.nc[k];
-          else if (ck >= g.nc[k]) ck -= g.nc[k];
-          cell += ck * mult;
-          mult *= g.nc[k];
-        }
-        for (int p = start[cell]; p < start[cell + 1]; p++) {
-          const int j = idx[p];
-          if (j == i) continue;
-          double d[3] = {0.0, 0.0, 0.0};
-          #pragma unroll
-          for (int k = 0; k < D; k++) {
-            double v = x[(size_t)j * D + k] - xi[k];
-            // minimum image; rint(v / L) is 0 whenever |v| < 0.49 L
-            if (!(fabs(v) < 0.49 * g.L[k])) v -= g.L[k] * rint(v / g.L[k]);
-            d[k] = v;
-          }
-          fn(j, d);
-        }
+// Neighbour list of one state.  TPP lanes per particle i: lane l takes the
+// members l, l + TPP, ... of each of the 3^D cells around i's cell (cells in
+// a fixed order, members in index order) that pass the float32 distance
+// screen and keeps them in its own sub-list nbr[(e * TPP + l) * N + i],
+// e < min(count, W); ncnt[l * N + i] = count.  maxcnt receives the largest
+// count (the caller enlarges W and repeats when it exceeds W).
+template <int D>
+__global__ void __launch_bounds__(BLK) k_adj_list(AdjArgs g, const double* __restrict__ x,
+                                                  const int* __restrict__ start,
+                                                  const int* __restrict__ idx,
+                                                  const float* __restrict__ xs, int W,
+                                                  int* __restrict__ nbr, int* __restrict__ ncnt,
+                                                  int* __restrict__ maxcnt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = t % TPP, i = t / TPP;
+  int cnt = 0;
+  if (i < g.N) {
+    int c[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    float xf[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      const double xk = x[(size_t)i * D + k];
+      xf[k] = (float)xk;
+      c[k] = cell_of(g, k, xk);
+      if (g.nc[k] >= 3) {
+        lo[k] = c[k] - 1;
+        hi[k] = c[k] + 1;
+      } else {
+        lo[k] = 0;
+        hi[k] = g.nc[k] - 1;
       }
+    }
+    for (int cz = lo[2]; cz <= hi[2]; cz++)
+      for (int cy = lo[1]; cy <= hi[1]; cy++)
+        for (int cx = lo[0]; cx <= hi[0]; cx++) {
+          const int cc[3] = {cx, cy, cz};
+          int cell = 0, mult = 1;
+#pragma unroll
+          for (int k = 0; k < D; k++) {
+            int ck = cc[k];
+            if (ck < 0) ck += g.nc[k];
+            else if (ck >= g.nc[k]) ck -= g.nc[k];
+            cell += ck * mult;
+            mult *= g.nc[k];
+          }
+          const int e = start[cell + 1];
+          for (int p = start[cell] + lane; p < e; p += TPP) {
+            float r2f = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+              float v = xs[(size_t)p * D + k] - xf[k];
+              v -= g.Lf[k] * rintf(v * g.Linvf[k]);
+              r2f += v * v;
+            }
+            if (r2f > g.cut2f) continue;
+            const int j = idx[p];
+            if (j == i) continue;
+            if (cnt < W) nbr[((size_t)cnt * TPP + lane) * g.N + i] = j;
+            cnt++;
+          }
+        }
+    ncnt[(size_t)lane * g.N + i] = cnt;
+  }
+  const int m = __reduce_max_sync(0xffffffffu, cnt);
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(maxcnt, m);
+}
+
+// Visit, on lane `lane` of the TPP lanes of particle i, the entries of its
+// sub-list, with the float64 minimum-image vector d = x_j - x_i.
+template <int D, class Fn>
+__device__ inline void for_list(const AdjArgs& g, const double* __restrict__ x,
+                                const int* __restrict__ nbr, const int* __restrict__ ncnt, int W,
+                                int i, const double* xi, int lane, Fn&& fn) {
+  const int cnt = min(ncnt[(size_t)lane * g.N + i], W);
+  for (int e = 0; e < cnt; e++) {
+    const int j = nbr[((size_t)e * TPP + lane) * g.N + i];
+    double d[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      double v = x[(size_t)j * D + k] - xi[k];
+      // minimum image; rint(v / L) is 0 whenever |v| < 0.49 L
+      if (!(fabs(v) < 0.49 * g.L[k])) v -= g.L[k] * rint(v / g.L[k]);
+      d[k] = v;
+    }
+    fn(j, d);
+  }
+}
+
+// Sum over the TPP lanes of one particle (xor tree: the same order on every
+// lane, so all lanes hold the same value).
+__device__ inline double lane_sum(double v) {
+#pragma unroll
+  for (int o = 1; o < TPP; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 // One state: loss terms (F_LOSS, accumulated per particle into lacc) and the
-// step to the next state (F_STEP).
-template <int D>
+// step to the next state (F_STEP).  TPP lanes per particle.
+template <int D, int FL>
 __global__ void __launch_bounds__(BLK) k_adj_step(AdjArgs g, const double* __restrict__ x,
-                                                  const int* __restrict__ start,
-                                                  const int* __restrict__ idx,
+                                                  const int* __restrict__ nbr,
+                                                  const int* __restrict__ ncnt, int W,
                                                   const int* __restrict__ types,
                                                   const double* __restrict__ noise,
                                                   double* __restrict__ x_out,
-                                                  double* __restrict__ lacc, int flags) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.N) return;
+                                                  double* __restrict__ lacc) {
+  __shared__ Law slaws[MAXL];
+  if (threadIdx.x < (unsigned)g.nlaws) slaws[threadIdx.x] = g.laws[threadIdx.x];
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = t % TPP;
+  const int i = min(t / TPP, g.N - 1);  // surplus lanes mirror the last particle
+  const bool own = t / TPP < g.N;
   const int ti = types[i];
   double xi[3] = {0.0, 0.0, 0.0};
-  #pragma unroll
+#pragma unroll
   for (int k = 0; k < D; k++) xi[k] = x[(size_t)i * D + k];
   double a[3] = {0.0, 0.0, 0.0};
   double loss = 0.0;
-  for_neighbours<D>(g, x, start, idx, i, xi, [&](int j, const double* d) {
+  for_list<D>(g, x, nbr, ncnt, W, i, xi, lane, [&](int j, const double* d) {
     const int tj = types[j];
     const unsigned int m = g.lawmask[ti * MAXT + tj];
     if (!m) return;
     double r2 = 0.0;
-    #pragma unroll
+#pragma unroll
     for (int k = 0; k < D; k++) r2 += d[k] * d[k];
-    const double r = sqrt(r2), ir = 1.0 / r;
-    for (int l = 0; l < g.nlaws; l++) {
-      if (!((m >> l) & 1)) continue;
-      const Law& w = g.laws[l];
+    const double ir = rsqrt(r2), r = r2 * ir;
+    // iteration q takes each lane's q-th law: lanes of different type
+    // pairs evaluate their first laws together
+    for (unsigned int mm = m; mm; mm &= mm - 1) {
+      const Law& w = slaws[__ffs(mm) - 1];
       if (!(r < w.rc)) continue;
-      const PairEval p = eval_law(w, r);
-      #pragma unroll
-      for (int k = 0; k < D; k++) a[k] += p.f * d[k] * ir;
+      const PairEval p = eval_law(w, r, ir);
+      const double fi = p.f * ir;
+#pragma unroll
+      for (int k = 0; k < D; k++) a[k] += fi * d[k];
       // each pair is seen from both ends: half of its loss on each
-      loss += 0.5 * (g.wU * (p.U - w.Uc) - g.wW * r * p.f);
+      if (FL & F_LOSS) loss += 0.5 * (g.wU * (p.U - w.Uc) - g.wW * r * p.f);
     }
   });
-  if (flags & F_LOSS) lacc[i] += loss;
-  if (flags & F_STEP) {
-    #pragma unroll
+#pragma unroll
+  for (int k = 0; k < D; k++) a[k] = lane_sum(a[k]);
+  if (FL & F_LOSS) loss = lane_sum(loss);
+  if (!own || lane != 0) return;
+  if (FL & F_LOSS) lacc[i] += loss;
+  if (FL & F_STEP) {
+#pragma unroll
     for (int k = 0; k < D; k++) {
       double v = xi[k];
       v += g.c[ti] * a[k];
@@ -298,89 +375,91 @@ __global__ void __launch_bounds__(BLK) k_adj_step(AdjArgs g, const double* __res
 
 // One state of the backward pass (see the file comment).  gpart[block][NG]
 // accumulates this CTA's parameter gradients over the steps, in step order.
-template <int D>
+template <int D, int FL>
 __global__ void __launch_bounds__(BLK) k_adj_back(AdjArgs g, const double* __restrict__ x,
-                                                  const int* __restrict__ start,
-                                                  const int* __restrict__ idx,
+                                                  const int* __restrict__ nbr,
+                                                  const int* __restrict__ ncnt, int W,
                                                   const int* __restrict__ types,
                                                   const double* __restrict__ lam_next,
                                                   double* __restrict__ lam_out,
-                                                  double* __restrict__ gpart, int flags) {
-  __shared__ double red[BLK / 32][NG];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double gp[NG];
-  for (int q = 0; q < NG; q++) gp[q] = 0.0;
-  if (i < g.N) {
-    const int ti = types[i];
-    double xi[3] = {0.0, 0.0, 0.0}, wi[3] = {0.0, 0.0, 0.0}, out[3] = {0.0, 0.0, 0.0};
-    #pragma unroll
+                                                  double* __restrict__ gpart) {
+  __shared__ Law slaws[MAXL];
+  __shared__ double sgp[NG][BLK];  // per-thread parameter gradients
+  if (threadIdx.x < (unsigned)g.nlaws) slaws[threadIdx.x] = g.laws[threadIdx.x];
+#pragma unroll
+  for (int q = 0; q < NG; q++) sgp[q][threadIdx.x] = 0.0;
+  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = t % TPP;
+  const int i = min(t / TPP, g.N - 1);
+  const bool own = t / TPP < g.N;
+  const int ti = types[i];
+  double xi[3] = {0.0, 0.0, 0.0}, wi[3] = {0.0, 0.0, 0.0}, out[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    xi[k] = x[(size_t)i * D + k];
+    if (FL & F_STEP) wi[k] = g.c[ti] * lam_next[(size_t)i * D + k];
+  }
+  for_list<D>(g, x, nbr, ncnt, W, i, xi, lane, [&](int j, const double* d) {
+    const int tj = types[j];
+    const unsigned int m = g.lawmask[ti * MAXT + tj];
+    if (!m) return;
+    double r2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; k++) r2 += d[k] * d[k];
+    const double ir = rsqrt(r2), r = r2 * ir;
+    double rh[3] = {0.0, 0.0, 0.0}, dw[3] = {0.0, 0.0, 0.0};
+    double rdw = 0.0;  // rhat . (w_j - w_i)
+#pragma unroll
     for (int k = 0; k < D; k++) {
-      xi[k] = x[(size_t)i * D + k];
-      if (flags & F_STEP) {
-        wi[k] = g.c[ti] * lam_next[(size_t)i * D + k];
-        out[k] = lam_next[(size_t)i * D + k];
+      rh[k] = d[k] * ir;
+      if (FL & F_STEP) {
+        dw[k] = g.c[tj] * lam_next[(size_t)j * D + k] - wi[k];
+        rdw += rh[k] * dw[k];
       }
     }
-    for_neighbours<D>(g, x, start, idx, i, xi, [&](int j, const double* d) {
-      const int tj = types[j];
-      const unsigned int m = g.lawmask[ti * MAXT + tj];
-      if (!m) return;
-      double r2 = 0.0;
-      #pragma unroll
-      for (int k = 0; k < D; k++) r2 += d[k] * d[k];
-      const double r = sqrt(r2), ir = 1.0 / r;
-      double rh[3] = {0.0, 0.0, 0.0}, dw[3] = {0.0, 0.0, 0.0};
-      double rdw = 0.0, rdwi = 0.0;  // rhat . (w_j - w_i), rhat . (w_i - w_j)
-      #pragma unroll
-      for (int k = 0; k < D; k++) {
-        rh[k] = d[k] * ir;
-        if (flags & F_STEP) {
-          dw[k] = g.c[tj] * lam_next[(size_t)j * D + k] - wi[k];
-          rdw += rh[k] * dw[k];
-        }
-      }
-      rdwi = -rdw;
+    // iteration q takes each lane's q-th law (see k_adj_step)
+    for (unsigned int mm = m; mm; mm &= mm - 1) {
+      const int l = __ffs(mm) - 1;
+      const Law& w = slaws[l];
+      if (!(r < w.rc)) continue;
+      const PairEval p = eval_law(w, r, ir);
+      if (FL & F_STEP) {
+        const double fr = p.f * ir;
 #pragma unroll
-      for (int l = 0; l < MAXL; l++) {
-        if (!((m >> l) & 1)) continue;
-        const Law& w = g.laws[l];
-        if (!(r < w.rc)) continue;
-        const PairEval p = eval_law(w, r);
-        if (flags & F_STEP) {
-          const double fr = p.f * ir;
-          #pragma unroll
-          for (int k = 0; k < D; k++)
-            out[k] += p.fp * rh[k] * rdw + fr * (dw[k] - rh[k] * rdw);
-        }
-        if (flags & F_LOSS) {
-          // d loss_pair / dr times d r / d x_i = -rhat
-          const double dl = g.wU * p.f - g.wW * (p.f + r * p.fp);
-          #pragma unroll
-          for (int k = 0; k < D; k++) out[k] -= dl * rh[k];
-        }
-        if (j > i) {
-          for (int q = 0; q < 2; q++) {
-            double v = 0.0;
-            if (flags & F_STEP) v += p.df[q] * rdwi;
-            if (flags & F_LOSS)
-              v += g.wU * (p.dU[q] - (q == 0 ? w.dUc_du0 : w.dUc_dr0)) - g.wW * r * p.df[q];
-            gp[2 * l + q] += v;
-          }
+        for (int k = 0; k < D; k++) out[k] += p.fp * rh[k] * rdw + fr * (dw[k] - rh[k] * rdw);
+      }
+      if (FL & F_LOSS) {
+        // d loss_pair / dr times d r / d x_i = -rhat
+        const double dl = g.wU * p.f - g.wW * (p.f + r * p.fp);
+#pragma unroll
+        for (int k = 0; k < D; k++) out[k] -= dl * rh[k];
+      }
+      if (j > i && own) {
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          double v = 0.0;
+          if (FL & F_STEP) v -= p.df[q] * rdw;  // df/dtheta rhat . (w_i - w_j)
+          if (FL & F_LOSS)
+            v += g.wU * (p.dU[q] - (q == 0 ? w.dUc_du0 : w.dUc_dr0)) - g.wW * r * p.df[q];
+          sgp[2 * l + q][threadIdx.x] += v;
         }
       }
-    });
-    #pragma unroll
-    for (int k = 0; k < D; k++) lam_out[(size_t)i * D + k] = out[k];
+    }
+  });
+#pragma unroll
+  for (int k = 0; k < D; k++) out[k] = lane_sum(out[k]);
+  if (own && lane == 0) {
+#pragma unroll
+    for (int k = 0; k < D; k++)
+      lam_out[(size_t)i * D + k] = out[k] + ((FL & F_STEP) ? lam_next[(size_t)i * D + k] : 0.0);
   }
-  // CTA sum of the parameter gradients (fixed shape), added to this CTA's slot
-  for (int q = 0; q < NG; q++)
-    for (int o = 16; o > 0; o >>= 1) gp[q] += __shfl_down_sync(0xffffffffu, gp[q], o);
-  if ((threadIdx.x & 31) == 0)
-    for (int q = 0; q < NG; q++) red[threadIdx.x >> 5][q] = gp[q];
+  // CTA sum of the parameter gradients in thread order, added to this CTA's
+  // slot
   __syncthreads();
-  if (threadIdx.x < NG) {
+  if (threadIdx.x < 2 * g.nlaws) {
     double v = 0.0;
-    for (int w = 0; w < BLK / 32; w++) v += red[w][threadIdx.x];
+    for (int u = 0; u < BLK; u++) v += sgp[threadIdx.x][u];
     gpart[(size_t)blockIdx.x * NG + threadIdx.x] += v;
   }
 }
@@ -410,6 +489,8 @@ __global__ void k_scale(double* v, size_t n, double f) {
 }
 
 unsigned nblk(int n) { return (unsigned)((n + BLK - 1) / BLK); }
+// CTAs of the pair kernels (TPP lanes per particle)
+unsigned pblk(int n) { return nblk(n * TPP); }
 
 }  // namespace
 
@@ -420,9 +501,13 @@ struct rdsim_adjoint {
   std::vector<rdsim_interaction> laws;
   int K = 1, E = 32;
   int* types = nullptr;
-  int *count = nullptr, *cursor = nullptr;
-  // cell lists of the segment's states: E + 1 slots of start[ncell + 1], idx[N]
-  int *seg_start = nullptr, *seg_idx = nullptr;
+  // cells of the state being listed (transient)
+  int *count = nullptr, *cursor = nullptr, *start = nullptr, *idx = nullptr;
+  float* xs = nullptr;             // [N][D] float32 positions in cell order
+  // neighbour lists of the segment's states: E + 1 slots of nbr[W][N], ncnt[N]
+  int W = 0;
+  int *seg_nbr = nullptr, *seg_ncnt = nullptr;
+  int* maxcnt = nullptr;
   double* seg_x = nullptr;         // [E][N][D] states of the current segment
   double* ckpt = nullptr;          // [nckpt][N][D] states 0, E, 2E, ...
   size_t ckpt_cap = 0;
@@ -441,54 +526,89 @@ void free_adj(rdsim_adjoint* h) {
   auto F = [](void* p) {
     if (p) cudaFree(p);
   };
-  F(h->types); F(h->count); F(h->cursor); F(h->seg_start); F(h->seg_idx); F(h->seg_x);
+  F(h->types); F(h->count); F(h->cursor); F(h->start); F(h->idx); F(h->xs);
+  F(h->seg_nbr); F(h->seg_ncnt); F(h->maxcnt); F(h->seg_x);
   F(h->ckpt); F(h->xT); F(h->lacc); F(h->lam[0]); F(h->lam[1]); F(h->gpart); F(h->red);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
-int* slot_start(rdsim_adjoint* h, int s) { return h->seg_start + (size_t)s * (h->g.ncell + 1); }
-int* slot_idx(rdsim_adjoint* h, int s) { return h->seg_idx + (size_t)s * h->g.N; }
+int* slot_nbr(rdsim_adjoint* h, int s) { return h->seg_nbr + (size_t)s * h->W * TPP * h->g.N; }
+int* slot_ncnt(rdsim_adjoint* h, int s) { return h->seg_ncnt + (size_t)s * TPP * h->g.N; }
 
-template <int D>
-void build_cells_d(rdsim_adjoint* h, const double* x, int slot) {
-  const AdjArgs& g = h->g;
-  k_bin<D><<<nblk(g.N), BLK, 0, h->stream>>>(g, x, h->count);
-  k_scan<<<1, SCAN_T, 0, h->stream>>>(h->count, g.ncell, slot_start(h, slot), h->cursor);
-  k_fill<D><<<nblk(g.N), BLK, 0, h->stream>>>(g, x, h->cursor, slot_idx(h, slot));
-  k_cell_sort<<<nblk(g.ncell), BLK, 0, h->stream>>>(g.ncell, slot_start(h, slot),
-                                                     slot_idx(h, slot), h->count);
+// (Re)allocates the neighbour-list slots for width W.
+int alloc_lists(rdsim_adjoint* h, int W) {
+  if (h->seg_nbr) cudaFree(h->seg_nbr);
+  h->seg_nbr = nullptr;
+  h->W = 0;
+  const size_t slots = (size_t)h->E + 1;
+  if (cudaMalloc(&h->seg_nbr, sizeof(int) * slots * W * TPP * h->g.N) != cudaSuccess)
+    return fail(RDSIM_ERR_NOMEM, "neighbour lists");
+  h->W = W;
+  return 0;
 }
 
-void build_cells(rdsim_adjoint* h, const double* x, int slot) {
-  if (h->g.D == 2) build_cells_d<2>(h, x, slot);
-  else if (h->g.D == 3) build_cells_d<3>(h, x, slot);
-  else build_cells_d<1>(h, x, slot);
+template <int D>
+void build_list_d(rdsim_adjoint* h, const double* x, int slot) {
+  const AdjArgs& g = h->g;
+  k_bin<D><<<nblk(g.N), BLK, 0, h->stream>>>(g, x, h->count);
+  k_scan<<<1, SCAN_T, 0, h->stream>>>(h->count, g.ncell, h->start, h->cursor);
+  k_fill<D><<<nblk(g.N), BLK, 0, h->stream>>>(g, x, h->cursor, h->idx);
+  k_cell_sort<D><<<nblk(g.ncell), BLK, 0, h->stream>>>(g.ncell, x, h->start, h->idx, h->xs,
+                                                        h->count);
+  k_adj_list<D><<<pblk(g.N), BLK, 0, h->stream>>>(g, x, h->start, h->idx, h->xs, h->W,
+                                                   slot_nbr(h, slot), slot_ncnt(h, slot),
+                                                   h->maxcnt);
+}
+
+// Cells and neighbour list of state x into list slot `slot`.
+void build_list(rdsim_adjoint* h, const double* x, int slot) {
+  if (h->g.D == 2) build_list_d<2>(h, x, slot);
+  else if (h->g.D == 3) build_list_d<3>(h, x, slot);
+  else build_list_d<1>(h, x, slot);
+}
+
+template <int D, int FL>
+void step_k(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out) {
+  k_adj_step<D, FL><<<pblk(h->g.N), BLK, 0, h->stream>>>(h->g, x, slot_nbr(h, slot),
+                                                          slot_ncnt(h, slot), h->W, h->types,
+                                                          noise, x_out, h->lacc);
+}
+
+template <int D>
+void step_d(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out,
+            int flags) {
+  if (flags == F_STEP) step_k<D, F_STEP>(h, x, slot, noise, x_out);
+  else if (flags == F_LOSS) step_k<D, F_LOSS>(h, x, slot, noise, x_out);
+  else step_k<D, F_STEP | F_LOSS>(h, x, slot, noise, x_out);
 }
 
 void step(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out,
           int flags) {
-  const unsigned g = nblk(h->g.N);
-  const int* st = slot_start(h, slot);
-  const int* ix = slot_idx(h, slot);
-  if (h->g.D == 2)
-    k_adj_step<2><<<g, BLK, 0, h->stream>>>(h->g, x, st, ix, h->types, noise, x_out, h->lacc, flags);
-  else if (h->g.D == 3)
-    k_adj_step<3><<<g, BLK, 0, h->stream>>>(h->g, x, st, ix, h->types, noise, x_out, h->lacc, flags);
-  else
-    k_adj_step<1><<<g, BLK, 0, h->stream>>>(h->g, x, st, ix, h->types, noise, x_out, h->lacc, flags);
+  if (h->g.D == 2) step_d<2>(h, x, slot, noise, x_out, flags);
+  else if (h->g.D == 3) step_d<3>(h, x, slot, noise, x_out, flags);
+  else step_d<1>(h, x, slot, noise, x_out, flags);
+}
+
+template <int D, int FL>
+void back_k(rdsim_adjoint* h, const double* x, int slot, const double* lam_next, double* lam_out) {
+  k_adj_back<D, FL><<<pblk(h->g.N), BLK, 0, h->stream>>>(h->g, x, slot_nbr(h, slot),
+                                                          slot_ncnt(h, slot), h->W, h->types,
+                                                          lam_next, lam_out, h->gpart);
+}
+
+template <int D>
+void back_d(rdsim_adjoint* h, const double* x, int slot, const double* lam_next, double* lam_out,
+            int flags) {
+  if (flags == F_STEP) back_k<D, F_STEP>(h, x, slot, lam_next, lam_out);
+  else if (flags == F_LOSS) back_k<D, F_LOSS>(h, x, slot, lam_next, lam_out);
+  else back_k<D, F_STEP | F_LOSS>(h, x, slot, lam_next, lam_out);
 }
 
 void back(rdsim_adjoint* h, const double* x, int slot, const double* lam_next, double* lam_out,
           int flags) {
-  const unsigned g = nblk(h->g.N);
-  const int* st = slot_start(h, slot);
-  const int* ix = slot_idx(h, slot);
-  if (h->g.D == 2)
-    k_adj_back<2><<<g, BLK, 0, h->stream>>>(h->g, x, st, ix, h->types, lam_next, lam_out, h->gpart, flags);
-  else if (h->g.D == 3)
-    k_adj_back<3><<<g, BLK, 0, h->stream>>>(h->g, x, st, ix, h->types, lam_next, lam_out, h->gpart, flags);
-  else
-    k_adj_back<1><<<g, BLK, 0, h->stream>>>(h->g, x, st, ix, h->types, lam_next, lam_out, h->gpart, flags);
+  if (h->g.D == 2) back_d<2>(h, x, slot, lam_next, lam_out, flags);
+  else if (h->g.D == 3) back_d<3>(h, x, slot, lam_next, lam_out, flags);
+  else back_d<1>(h, x, slot, lam_next, lam_out, flags);
 }
 
 }  // namespace
@@ -538,10 +658,20 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
     if (nc < 3) nc = 1;
     g.nc[k] = nc;
     g.L[k] = s->L[k];
+    g.Lf[k] = (float)s->L[k];
+    g.Linvf[k] = (float)(1.0 / s->L[k]);
     g.cellinv[k] = nc / s->L[k];
     V *= s->L[k];
   }
   for (int k = D; k < 3; k++) g.nc[k] = 1;
+  {
+    // float32 screen of candidate pairs: float32 positions and minimum image
+    // err by a few 1e-7 L per coordinate
+    double Lmax = 0.0;
+    for (int k = 0; k < D; k++) Lmax = std::max(Lmax, s->L[k]);
+    const double cut = rc_max + 1e-3 + 1e-6 * Lmax;
+    g.cut2f = (float)(cut * cut * (1.0 + 1e-6));
+  }
   g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
   for (int t = 0; t < s->n_types; t++) {
     const double Dt = s->mobility[t];
@@ -572,16 +702,30 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
   bool ok = cudaMalloc(&h->types, sizeof(int) * N) == cudaSuccess &&
             cudaMalloc(&h->count, sizeof(int) * g.ncell) == cudaSuccess &&
             cudaMalloc(&h->cursor, sizeof(int) * g.ncell) == cudaSuccess &&
-            cudaMalloc(&h->seg_start, sizeof(int) * slots * (g.ncell + 1)) == cudaSuccess &&
-            cudaMalloc(&h->seg_idx, sizeof(int) * slots * N) == cudaSuccess &&
+            cudaMalloc(&h->start, sizeof(int) * (g.ncell + 1)) == cudaSuccess &&
+            cudaMalloc(&h->idx, sizeof(int) * N) == cudaSuccess &&
+            cudaMalloc(&h->xs, sizeof(float) * nd) == cudaSuccess &&
+            cudaMalloc(&h->seg_ncnt, sizeof(int) * slots * TPP * N) == cudaSuccess &&
+            cudaMalloc(&h->maxcnt, sizeof(int)) == cudaSuccess &&
             cudaMalloc(&h->seg_x, sizeof(double) * h->E * nd) == cudaSuccess &&
             cudaMalloc(&h->xT, sizeof(double) * nd) == cudaSuccess &&
             cudaMalloc(&h->lacc, sizeof(double) * N) == cudaSuccess &&
             cudaMalloc(&h->lam[0], sizeof(double) * nd) == cudaSuccess &&
             cudaMalloc(&h->lam[1], sizeof(double) * nd) == cudaSuccess &&
-            cudaMalloc(&h->gpart, sizeof(double) * nblk(N) * NG) == cudaSuccess &&
+            cudaMalloc(&h->gpart, sizeof(double) * pblk(N) * NG) == cudaSuccess &&
             cudaMalloc(&h->red, sizeof(double) * NG) == cudaSuccess;
   if (!ok) return bail(fail(RDSIM_ERR_NOMEM, "device allocation failed"));
+  {
+    // sub-list width: twice the expected number of particles within the
+    // screen distance per lane, plus a margin (a forward pass that finds
+    // more widens it)
+    const double cut = std::sqrt((double)g.cut2f);
+    const double ball = D == 1 ? 2.0 * cut : (D == 2 ? M_PI * cut * cut : 4.0 / 3.0 * M_PI * cut * cut * cut);
+    const double expect = std::min((double)N, N / V * ball) / TPP;
+    const int W = (int)(2.0 * expect) + 8;
+    int rc = alloc_lists(h, std::min(W, N));
+    if (rc) return bail(rc);
+  }
   if (cudaMemcpyAsync(h->types, types.data(), sizeof(int) * N, cudaMemcpyHostToDevice, h->stream) !=
           cudaSuccess ||
       cudaMemsetAsync(h->count, 0, sizeof(int) * g.ncell, h->stream) != cudaSuccess ||
@@ -621,7 +765,8 @@ int rdsim_adjoint_forward(rdsim_adjoint* h, const double* x0, const double* para
     w.r0 = params[2 * l + 1];
     w.rc = it.rc;
     if (!(w.r0 > 0)) return fail(RDSIM_ERR_ARG, "r0 must be positive");
-    const PairEval p = eval_law(w, w.rc);
+    w.ir0 = 1.0 / w.r0;
+    const PairEval p = eval_law(w, w.rc, 1.0 / w.rc);
     w.Uc = p.U;
     w.dUc_du0 = p.dU[0];
     w.dUc_dr0 = p.dU[1];
@@ -637,26 +782,38 @@ int rdsim_adjoint_forward(rdsim_adjoint* h, const double* x0, const double* para
       return fail(RDSIM_ERR_NOMEM, "checkpoint buffer");
     h->ckpt_cap = nck * nd;
   }
-  CK(cudaMemsetAsync(h->lacc, 0, sizeof(double) * N, h->stream));
-  CK(cudaMemcpyAsync(h->ckpt, x0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, h->stream));
-  // states between checkpoints alternate between seg_x[0] and seg_x[1] (the
-  // segment buffer is free during the forward pass; E >= 2 there)
-  const double* cur = h->ckpt;
-  const int slot = E;  // cell-list slot of the forward pass
-  for (int n = 0; n <= n_steps; n++) {
-    int flags = n >= n_steps - h->K + 1 ? F_LOSS : 0;
-    double* nxt = nullptr;
-    if (n < n_steps) {
-      flags |= F_STEP;
-      const int m = n + 1;
-      nxt = m % E == 0 ? h->ckpt + (size_t)(m / E) * nd : h->seg_x + (size_t)(m & 1) * nd;
+  const double* cur = nullptr;
+  for (int attempt = 0;; attempt++) {
+    CK(cudaMemsetAsync(h->lacc, 0, sizeof(double) * N, h->stream));
+    CK(cudaMemsetAsync(h->maxcnt, 0, sizeof(int), h->stream));
+    CK(cudaMemcpyAsync(h->ckpt, x0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, h->stream));
+    // states between checkpoints alternate between seg_x[0] and seg_x[1]
+    // (the segment buffer is free during the forward pass; E >= 2 there)
+    cur = h->ckpt;
+    const int slot = E;  // list slot of the forward pass
+    for (int n = 0; n <= n_steps; n++) {
+      int flags = n >= n_steps - h->K + 1 ? F_LOSS : 0;
+      double* nxt = nullptr;
+      if (n < n_steps) {
+        flags |= F_STEP;
+        const int m = n + 1;
+        nxt = m % E == 0 ? h->ckpt + (size_t)(m / E) * nd : h->seg_x + (size_t)(m & 1) * nd;
+      }
+      build_list(h, cur, slot);
+      step(h, cur, slot, n < n_steps ? xi + (size_t)n * nd : nullptr, nxt, flags);
+      if (nxt) cur = nxt;
     }
-    build_cells(h, cur, slot);
-    step(h, cur, slot, n < n_steps ? xi + (size_t)n * nd : nullptr, nxt, flags);
-    if (nxt) cur = nxt;
+    CK(cudaGetLastError());
+    int mx = 0;
+    CK(cudaMemcpyAsync(&mx, h->maxcnt, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (mx <= h->W) break;
+    // a list row overflowed: widen the lists and run the pass again
+    if (attempt > 0) return fail(RDSIM_ERR_CAPACITY, "neighbour list overflow");
+    int rc = alloc_lists(h, std::min(N, mx + mx / 4 + 4));
+    if (rc) return rc;
   }
   if (cur != h->xT) CK(cudaMemcpyAsync(h->xT, cur, sizeof(double) * nd, cudaMemcpyDeviceToDevice, h->stream));
-  CK(cudaGetLastError());
   k_sum_rows<<<1, BLK, 0, h->stream>>>(h->lacc, N, 1, h->red);
   CK(cudaMemcpyAsync(loss, h->red, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (x_final) CK(cudaMemcpyAsync(x_final, h->xT, sizeof(double) * nd, cudaMemcpyDeviceToDevice, h->stream));
@@ -673,7 +830,7 @@ int rdsim_adjoint_backward(rdsim_adjoint* h, double dloss, double* grad_x0, doub
   const AdjArgs& g = h->g;
   const int N = g.N, D = g.D, E = h->E, T = h->T;
   const size_t nd = (size_t)N * D;
-  CK(cudaMemsetAsync(h->gpart, 0, sizeof(double) * nblk(N) * NG, h->stream));
+  CK(cudaMemsetAsync(h->gpart, 0, sizeof(double) * pblk(N) * NG, h->stream));
   CK(cudaMemsetAsync(h->lam[0], 0, sizeof(double) * nd, h->stream));
   int cur = 0;     // lam[cur] holds lambda_{n+1}
   int seg = -1;    // base step of the states held in seg_x
@@ -683,20 +840,20 @@ int rdsim_adjoint_backward(rdsim_adjoint* h, double dloss, double* grad_x0, doub
     if (n == T) {
       x = h->xT;
       slot = E;
-      build_cells(h, x, slot);
+      build_list(h, x, slot);
     } else {
       const int b = (n / E) * E;
       if (b != seg) {
         // recompute states b .. b + E - 1 (those below T) from checkpoint b / E
         CK(cudaMemcpyAsync(h->seg_x, h->ckpt + (size_t)(b / E) * nd, sizeof(double) * nd,
                            cudaMemcpyDeviceToDevice, h->stream));
-        build_cells(h, h->seg_x, 0);
+        build_list(h, h->seg_x, 0);
         const int last = std::min(b + E - 1, T - 1);
         for (int q = 1; q <= last - b; q++) {
           const double* prev = h->seg_x + (size_t)(q - 1) * nd;
           double* nx = h->seg_x + (size_t)q * nd;
           step(h, prev, q - 1, h->xi + (size_t)(b + q - 1) * nd, nx, F_STEP);
-          build_cells(h, nx, q);
+          build_list(h, nx, q);
         }
         seg = b;
       }
@@ -709,7 +866,7 @@ int rdsim_adjoint_backward(rdsim_adjoint* h, double dloss, double* grad_x0, doub
     cur = 1 - cur;
   }
   CK(cudaGetLastError());
-  k_sum_rows<<<1, BLK, 0, h->stream>>>(h->gpart, (int)nblk(N), NG, h->red);
+  k_sum_rows<<<1, BLK, 0, h->stream>>>(h->gpart, (int)pblk(N), NG, h->red);
   double gsum[NG];
   CK(cudaMemcpyAsync(gsum, h->red, sizeof gsum, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(grad_x0, h->lam[cur], sizeof(double) * nd, cudaMemcpyDeviceToDevice,
