@@ -194,9 +194,12 @@ def ensemble_comparison(local, steps=100, n_systems=512):
     import torch
     from pyrdsim_gb300 import workloads
     from pyrdsim_gb300.engine import Engine
+    from pyrdsim_gb300.autotune import autotune
     sds = workloads.ensemble(n_systems=n_systems)
     total = sum(s.n_particles for s in sds)
-    batch = Engine(sds, device=local)
+    tuned = autotune(sds, device=local, steps=steps)
+    batch = Engine(sds, device=local, skin=tuned["skin"],
+                   threads_per_particle=tuned["threads_per_particle"] or 0)
     batch.step(steps // 2)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -219,6 +222,7 @@ def ensemble_comparison(local, steps=100, n_systems=512):
     p = total * steps / t_p
     return {"n_systems": n_systems, "n_particles": total, "steps": steps,
             "batched": b, "plain_per_system": p, "speedup": b / p, "unit": UNIT,
+            "batched_options": tuned,
             "workload": "512 systems, N log-uniform [256, 16384], density U[0.2, 0.7], "
                         "kT U[0.5, 2], LJ or Yukawa, half with two-state reactions"}
 

@@ -107,9 +107,18 @@ class Engine:
     """
 
     def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, use_graphs=True,
-                 list_width=0, reaction_prefilter=None):
+                 list_width=0, reaction_prefilter=None, autotune=False):
+        """``autotune=True`` picks ``skin`` and ``threads_per_particle`` by
+        timing short runs of this batch (:mod:`pyrdsim_gb300.autotune`,
+        cached per workload)."""
         self.lib = load_library()
         self.systems = list(systems)
+        if autotune:
+            from .autotune import autotune as _tune
+            best = _tune(self.systems, device=device)
+            skin = best["skin"]
+            threads_per_particle = best["threads_per_particle"] or 0
+        self.options = {"skin": skin, "threads_per_particle": threads_per_particle}
         self.D = self.systems[0].model.N_dim
         self.offsets = np.cumsum([0] + [s.n_particles for s in self.systems])
         self.N = int(self.offsets[-1])
