@@ -7,7 +7,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_autotuned_options_keep_results(tmp_path):
+def test_autotuned_options_keep_results(tmp_path, monkeypatch):
     from pyrdsim_gb300 import autotune, workloads
     from pyrdsim_gb300.engine import Engine
     sds = [workloads.lj_fluid(n=4096), workloads.lj_fluid(n=1024, seed=3)]
@@ -19,8 +19,8 @@ def test_autotuned_options_keep_results(tmp_path):
     eng = Engine(sds, skin=best["skin"], threads_per_particle=best["threads_per_particle"])
     a = eng.drift()
     assert np.linalg.norm(a - ref) <= 1e-6 * np.linalg.norm(ref)
-    # the Engine option reads the cache written above
-    import os
-    os.environ["XDG_CACHE_HOME"] = str(tmp_path / "xdg")
+    # Engine(autotune=True) tunes into the user cache (here a fresh one)
+    monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path / "xdg"))
     tuned = Engine(sds, autotune=True)
+    assert (tmp_path / "xdg" / "pyrdsim_gb300" / "autotune.json").exists()
     assert tuned.options["threads_per_particle"] in (0,) + autotune.LANES
