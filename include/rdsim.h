@@ -114,7 +114,10 @@ typedef struct {
   int32_t cell_length_ratio;       /* pyrdsim.pyx:327, 575                    */
   int32_t neighbor_list_update_frequency; /* pyrdsim.pyx:325, 584          */
   int32_t angle_is_pi;             /* +1 / -1: the theta0 == pi flag that every
-                                      angle term reads (pyrdsim.pyx:1350-1401) */
+                                      angle term reads (pyrdsim.pyx:1350-1401:
+                                      the flag of the last angle defined);
+                                      0: each angle term uses its own
+                                      theta0 == pi test (no late binding)   */
   int32_t n_interactions, n_reactions, n_templates, n_terms;
   const double* tau_by_tauD;       /* [n_types]                               */
   const rdsim_interaction* interactions; /* file order                       */

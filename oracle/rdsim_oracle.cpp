@@ -40,6 +40,7 @@ struct BondF {
 struct AngleF {
   int i1, i2, i3;
   double k0, theta0, thr;
+  int pi;  // +1 if theta0 == pi (np.isclose, pyx:1333-1338), else -1
 };
 
 }  // namespace
@@ -139,7 +140,8 @@ struct oracle_handle {
           bonded[std::min(i1, i2)].insert(std::max(i1, i2));
         } else if (tm.kind == RDSIM_TERM_ANGLE) {
           int i1 = tm.i + j, i2 = tm.j + j, i3 = tm.k + j;
-          angles.push_back({i1, i2, i3, tm.k0, tm.p0, tm.p0 - 0.1});
+          angles.push_back({i1, i2, i3, tm.k0, tm.p0, tm.p0 - 0.1,
+                            std::fabs(tm.p0 - M_PI) <= 1e-5 + 1e-5 * M_PI ? 1 : -1});
           bonded[std::min(i1, i2)].insert(std::max(i1, i2));
           bonded[std::min(i2, i3)].insert(std::max(i2, i3));
         }
@@ -334,7 +336,8 @@ struct oracle_handle {
         theta = std::acos(h);
       }
       double prefac;
-      if (angle_is_pi > 0) {
+      // angle_is_pi == 0: each term's own flag instead of the late-bound one
+      if (angle_is_pi != 0 ? angle_is_pi > 0 : an.pi > 0) {
         if (theta < an.thr)
           prefac = an.k0 * (theta - an.theta0) / (std::sqrt(1. - std::pow(h, 2.0)));
         else

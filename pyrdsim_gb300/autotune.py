@@ -23,7 +23,10 @@ import time
 import numpy as np
 
 LANES = (1, 2, 4, 8)
-SKIN_FACTORS = (0.5, 0.75, 1.0, 1.5)
+# The engine's automatic skin covers the diffusion of a rebuild period with a
+# wide margin; smaller skins can fail the displacement check on long runs, so
+# only larger ones (longer lists, larger cells) are tried.
+SKIN_FACTORS = (1.0, 1.25, 1.5)
 
 
 def default_cache_path():
@@ -60,9 +63,12 @@ def candidates(auto_skin):
 
 def _time_engine(systems, device, opts, steps):
     """Particle-steps per second of `steps` Philox steps (after a warm-up of
-    one rebuild period and graph capture)."""
-    from .engine import Engine
-    eng = Engine(systems, device=device, **opts)
+    one rebuild period and graph capture); 0 if the engine reports an error."""
+    from .engine import Engine, EngineError
+    try:
+        eng = Engine(systems, device=device, **opts)
+    except EngineError:
+        return 0.0
     try:
         freq = max(1, systems[0].model.neighbor_list_update_frequency)
         eng.step(2 * freq)
@@ -72,6 +78,8 @@ def _time_engine(systems, device, opts, steps):
         eng.state()
         dt = time.perf_counter() - t0
         return eng.N * steps / dt
+    except EngineError:
+        return 0.0
     finally:
         eng.close()
 

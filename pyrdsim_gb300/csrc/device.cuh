@@ -58,7 +58,8 @@ struct RxDev {
 
 struct TermDev {                  // bonded term; angles in radians
   int kind, i, j, k;
-  float p0, k0, thr, pad;
+  float p0, k0, thr;
+  float pi;                       // angle: +1 if its theta0 == pi, else -1
 };
 
 struct TmplDev {

@@ -1000,6 +1000,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
           d.p0 = (float)tr.p0;
           d.k0 = (float)tr.k0;
           d.thr = (float)(tr.p0 - 0.1);
+          d.pi = std::fabs(tr.p0 - M_PI) <= 1e-5 + 1e-5 * M_PI ? 1.f : -1.f;  // np.isclose
           int ti = (int)terms.size();
           terms.push_back(d);
           oterms.push_back(tr);

@@ -348,7 +348,10 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
       // where acos(h) loses half its digits in float32
       const float theta = atan2f(sn, c);
       float prefac;
-      if (s.angle_is_pi > 0 && !(theta < tr.thr)) {
+      // the expansion about pi: all angles follow the flag of the last angle
+      // defined (pyrdsim.pyx:1401), or each its own with angle_is_pi == 0
+      const bool pi_branch = s.angle_is_pi != 0 ? s.angle_is_pi > 0 : tr.pi > 0.f;
+      if (pi_branch && !(theta < tr.thr)) {
         const float dt_ = theta - tr.p0, d2_ = dt_ * dt_;
         prefac = -tr.k0 / (1.0f - d2_ / 6.0f + d2_ * d2_ / 120.0f);
       } else {

@@ -260,7 +260,10 @@ class SystemData:
     """Keeps the numpy arrays and ctypes tables behind one ``rdsim_system``."""
 
     def __init__(self, model: Model, x, particle_types, molecule_ids,
-                 first_index_of_molecule, seed=None):
+                 first_index_of_molecule, seed=None, angle_theta0_per_term=False):
+        """``angle_theta0_per_term``: every angle term uses its own theta0 ==
+        pi test instead of the reference's late-bound flag of the last angle
+        defined (pyrdsim.pyx:1401)."""
         self.model = model
         self.x = np.ascontiguousarray(x, dtype=np.float64)
         self.types = np.ascontiguousarray(particle_types, dtype=np.int32)
@@ -282,7 +285,8 @@ class SystemData:
         s.rs = model.rs
         s.cell_length_ratio = model.cell_length_ratio
         s.neighbor_list_update_frequency = model.neighbor_list_update_frequency
-        s.angle_is_pi = model.angle_is_pi(self.molecule_ids, self.first_index)
+        s.angle_is_pi = 0 if angle_theta0_per_term else \
+            model.angle_is_pi(self.molecule_ids, self.first_index)
         s.n_interactions = len(model.interactions)
         s.n_reactions = len(model.reactions)
         s.n_templates = n_tmpl

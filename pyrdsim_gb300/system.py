@@ -19,7 +19,9 @@ Differences, all deliberate:
   keeps pairs listed at earlier rebuilds);
 * GPU options are extra dictionary keys starting with ``gpu_``:
   ``gpu_device``, ``gpu_skin``, ``gpu_threads_per_particle``,
-  ``gpu_list_width``.
+  ``gpu_list_width``, and ``gpu_angle_theta0_per_term`` (True: each angle
+  uses its own theta0 == pi test, not the late-bound flag of the last angle
+  defined, pyrdsim.pyx:1401).
 """
 from __future__ import annotations
 
@@ -170,7 +172,9 @@ class system:  # noqa: N801  (the reference's class name)
             self._load_initial_conditions()
         N, D = self.x.shape
         sd = model.SystemData(m, self.x, self.particle_types, self.molecule_ids,
-                              self.first_index_of_molecule)
+                              self.first_index_of_molecule,
+                              angle_theta0_per_term=bool(self._gpu.get("angle_theta0_per_term",
+                                                                        False)))
         if verbose:
             print("Loading and processing initial conditions..done", end="\n")
             print("Creating neighbor list and evaluating drift..", end="\r")

@@ -230,3 +230,31 @@ def mixed_lj_yukawa_laws(w):
     out = [law("lj", pr, p[q, 0], p[q, 1], w["rc_lj"]) for q, pr in enumerate(w["pairs"])]
     out.append(law("yukawa", (1, 1), p[3, 0], p[3, 1], w["rc_yukawa"]))
     return out
+
+
+def inhibited_mixture(n=4096, rho=0.45, seed=6, dt=1e-4):
+    """Three species in a periodic box (WCA between all pairs): constant
+    activation 0 -> 1 (rate 20), locally inhibited 1 -> 2 (rate 40, minus 15
+    per inhibitor of type 0 or 2 within 1.6: both inhibitor fields used),
+    constant decay 2 -> 0 (rate 10).  Exercises the inhibited propensity with
+    its clamp at zero at scale."""
+    rng = np.random.default_rng(seed)
+    L = float(np.sqrt(n / rho))
+    inter = [{"type": "lj", "pair": [a, b], "u0": 1.0, "r0": WCA_R0, "rc": WCA_R0, "n": 6}
+             for a in range(3) for b in range(a, 3)]
+    params = {
+        "n_dim": 2, "l": np.array([L, L]), "periodic": np.array([1.0, 1.0]),
+        "dt": dt, "n_steps": 1000, "n_out": 1000000, "tau_by_taud": np.array([1.0, 1.0, 1.0]),
+        "seed": seed, "interactions": inter,
+        "reactions": [
+            {"type": "linear", "reactant": 0, "product": 1, "rate": 20.0},
+            {"type": "locally_inhibited", "reactant": 1, "product": 2, "rate": 40.0,
+             "rate_decrease": 15.0, "inhibitor": 0, "inhibitor2": 2, "r0": 1.6},
+            {"type": "linear", "reactant": 2, "product": 0, "rate": 10.0},
+        ],
+    }
+    m = model.Model.from_dict(params)
+    x = jittered_lattice(n, [L, L], rng)
+    types = rng.integers(0, 3, n).astype(np.int32)
+    mol, first = _single_atoms(n)
+    return model.SystemData(m, x, types, mol, first)

@@ -37,8 +37,9 @@ def in_deck(texts):
             os.chdir(cwd)
 
 
-def system_from_deck(texts, seed, overrides=None):
-    """Model + SystemData for a deck given as texts (parsed like the reference)."""
+def system_from_deck(texts, seed, overrides=None, **sd_kw):
+    """Model + SystemData for a deck given as texts (parsed like the reference);
+    ``sd_kw`` goes to SystemData."""
     params = {"seed": seed}
     if overrides:
         params.update(overrides)
@@ -46,7 +47,7 @@ def system_from_deck(texts, seed, overrides=None):
         m = model.Model(params)
         x, mol, types, first = decks.load_initial_conditions(
             m.initial_conditions_filename, m.N_dim, m.N_species, tuple(m.comment_chars))
-    return model.SystemData(m, x, types, mol, first)
+    return model.SystemData(m, x, types, mol, first, **sd_kw)
 
 
 def pair_set(pairs):

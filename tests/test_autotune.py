@@ -11,14 +11,14 @@ def test_autotune_takes_the_fastest_candidate_and_caches(tmp_path):
     def measure(opts):
         seen.append(dict(opts))
         rate = {1: 1.0, 2: 3.0, 4: 2.0, 8: 0.5}[opts["threads_per_particle"]]
-        return rate * (1.2 if opts["skin"] == 0.75 else 1.0)
+        return rate * (1.2 if opts["skin"] == 1.25 else 1.0)
 
     path = str(tmp_path / "cache.json")
     best = autotune.autotune(sds, cache_path=path, measure=measure)
-    assert best == {"threads_per_particle": 2, "skin": 0.75}
+    assert best == {"threads_per_particle": 2, "skin": 1.25}
     # every lane count with the automatic skin, then the scaled skins at 2 lanes
     assert [o["threads_per_particle"] for o in seen[:4]] == [1, 2, 4, 8]
-    assert all(o["threads_per_particle"] == 2 for o in seen[4:]) and len(seen) == 7
+    assert all(o["threads_per_particle"] == 2 for o in seen[4:]) and len(seen) == 6
     data = json.load(open(path))
     assert len(data) == 1 and list(data.values())[0]["options"] == best
     # a cached workload is not measured again

@@ -259,3 +259,59 @@ def test_reaction_prefilter_is_exact(case):
         changed += int((ta != prev).sum())
         prev = ta
     assert changed >= 5, "too few reactions to test the prefilter"
+
+
+def test_per_term_angle_flag_matches_oracle():
+    """angle_is_pi = 0 (each angle its own theta0 == pi test) on the deck
+    that mixes 180- and 120-degree angles: drift and 100 injected steps."""
+    fx = load_fixture("angle_pi")
+    sd = system_from_deck(deck_dict(fx), int(fx["seed"]), angle_theta0_per_term=True)
+    eng = _engine([sd])
+    orc = _oracle(sd)
+    norm, per = drift_errors(eng.drift(), orc.drift())
+    assert norm <= FORCE_RTOL and per <= FORCE_RTOL, (norm, per)
+    n, D = sd.n_particles, sd.model.N_dim
+    rng = np.random.default_rng(77)
+    xi = rng.standard_normal((100, n, D))
+    u = rng.random((100, n))
+    eng.step(100, xi=xi, u1=u, u2=u)
+    orc.step(100, xi=xi, u1=u, u2=u)
+    xg, tg = eng.state()
+    xo, to = orc.state()
+    d = min_image(xg - xo, sd)
+    assert (np.abs(d) <= POS_RTOL * np.maximum(np.abs(xo), 1.0)).all(), np.abs(d).max()
+    # the late-bound flag gives a different drift on this deck
+    quirk = _engine([_case("angle_pi")[1]])
+    assert np.abs(quirk.drift() - eng.drift()).max() > 1e-3
+
+
+def test_inhibited_reactions_at_scale():
+    """4,096 particles, three species, a locally inhibited reaction with both
+    inhibitor fields (propensities clamped at zero): 50 steps with injected
+    normals and uniforms; types bit-exact, positions within 1e-6, and the
+    propensities of the final state bit-exact."""
+    from pyrdsim_gb300 import workloads
+    sd = workloads.inhibited_mixture(n=4096)
+    n, D = sd.n_particles, sd.model.N_dim
+    rng = np.random.default_rng(31)
+    xi = rng.standard_normal((50, n, D))
+    u1 = rng.random((50, n))
+    u2 = rng.random((50, n))
+    eng = _engine([sd])
+    orc = _oracle(sd)
+    t0 = eng.state()[1].copy()
+    for c in range(5):
+        sl = slice(10 * c, 10 * (c + 1))
+        eng.step(10, xi=xi[sl], u1=u1[sl], u2=u2[sl])
+        orc.step(10, xi=xi[sl], u1=u1[sl], u2=u2[sl])
+    xg, tg = eng.state()
+    xo, to = orc.state()
+    np.testing.assert_array_equal(tg, to)
+    assert (tg != t0).sum() > 100
+    d = min_image(xg - xo, sd)
+    assert (np.abs(d) <= POS_RTOL * np.maximum(np.abs(xo), 1.0)).all(), np.abs(d).max()
+    eng.set_state(xo, to)
+    orc.set_state(xo, to)
+    r = orc.reaction_rates(recompute=True)
+    np.testing.assert_array_equal(eng.reaction_rates(), r)
+    assert (r == 0).any() and (r == 25.0).any() and (r == 10.0).any()

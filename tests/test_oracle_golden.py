@@ -137,3 +137,30 @@ def test_rdf_oracle_counts_every_pair_once():
     ref, _ = np.histogram(r[r < r_max], bins=50, range=(0.0, r_max))
     assert c.sum() == (r < r_max).sum()
     assert np.abs(c - ref).sum() <= 2  # numpy's bin edges round differently
+
+
+def test_per_term_angle_flag_makes_every_angle_a_gradient():
+    """With angle_is_pi = 0 every angle term takes its own theta0 == pi
+    branch, so the drift is -grad U for every particle of the deck whose
+    120-degree angles the late-bound flag sends through the expansion about
+    pi."""
+    fx = load_fixture("angle_pi")
+    sd = system_from_deck(deck_dict(fx), int(fx["seed"]), angle_theta0_per_term=True)
+    assert sd.struct.angle_is_pi == 0
+    o = Oracle(sd, history_quirk=False)
+    x0, t0 = o.state()
+    a = o.drift()
+    h = 1e-6
+    fd = np.zeros_like(a)
+    for i in range(sd.n_particles):
+        for k in range(sd.model.N_dim):
+            x = x0.copy()
+            x[i, k] += h
+            o.set_state(x, t0)
+            ep = _total_energy(o)
+            x[i, k] -= 2 * h
+            o.set_state(x, t0)
+            em = _total_energy(o)
+            fd[i, k] = -(ep - em) / (2 * h)
+    scale = max(np.abs(a).max(), 1.0)
+    assert np.abs(fd - a).max() <= 1e-5 * scale
