@@ -235,8 +235,58 @@ class system:  # noqa: N801  (the reference's class name)
             "first_index_of_molecule": self.first_index_of_molecule,
         }
 
-    def create_initial_conditions(self, *args, **kwargs):  # pyrdsim.pyx:2634
-        raise NotImplementedError(
-            "create_initial_conditions (CMA-ES molecule search and random insertion) is "
-            "set-up code outside the simulation step; generate initial conditions with the "
-            "reference or pyrdsim_gb300.workloads")
+    def create_initial_conditions(self, N_particles, particle_types,
+                                  reference_configurations=None,
+                                  min_distance_threshold=None,
+                                  min_distance_threshold_sim=None, relax=True):
+        """pyrdsim.pyx:2634-2828: place N_particles[molecule_id] molecules of
+        each type (atom types particle_types[molecule_id]) at random, each at
+        the best of 1000 random poses for the distance of its first atom to
+        the first atoms already placed, write the initial-condition file and
+        relax the system with ``simulate`` (see
+        :mod:`pyrdsim_gb300.initial_conditions` for what differs from the
+        reference).  Returns the array (molecule number, index in molecule,
+        molecule id, particle type, positions)."""
+        from . import initial_conditions as ic
+        m = self._model
+        if min_distance_threshold is None:
+            min_distance_threshold = m.rs / 4.
+        if min_distance_threshold_sim is None:
+            min_distance_threshold_sim = m.rs / 10.
+        D = m.N_dim
+        n_atoms = {i: int(m.molecule_parameters[i]["n_atoms"]) for i in m.molecule_interactions}
+        rng = np.random.default_rng(m.seed)
+        if not reference_configurations:
+            refs = {i: ic.create_reference_molecule(m.molecule_interactions[i], n_atoms[i], D, rng)
+                    for i in m.molecule_interactions}
+        else:
+            refs = {}
+            for i, filename in reference_configurations.items():
+                refs[i] = np.atleast_2d(np.genfromtxt(filename))
+                if len(refs[i]) != n_atoms[i]:
+                    raise RuntimeError(("Reference configuration for molecule {0}"
+                                        " has {1} atoms, but interaction parameters for that"
+                                        " molecule demand {2} atoms").format(
+                                            i, len(refs[i]), n_atoms[i]))
+        out = ic.generate(N_particles, particle_types, n_atoms, refs, m.L, D, rng,
+                          min_distance_threshold)
+        self._set_state_from_array(out)
+        self.write_current_state_to_text_file(filename=m.initial_conditions_filename)
+        if relax and len(self.first_index_of_molecule) > 3:
+            result = self.simulate(verbose=False, random_force=True)
+            relaxed = result["x"]
+            min_dist = self._engine.observables()["min_distance"]
+            if np.isnan(relaxed).any() or min_dist < min_distance_threshold_sim:
+                raise RuntimeError("Min distance {0} below threshold {1} after relaxation".format(
+                    min_dist, min_distance_threshold_sim))
+            out[:, 4:] = relaxed
+            self._set_state_from_array(out)
+            self.write_current_state_to_text_file(filename=m.initial_conditions_filename)
+        return out
+
+    def _set_state_from_array(self, out):
+        self.molecule_ids = np.array(out[:, :3], dtype=np.intc)
+        self.particle_types = np.array(out[:, 3], dtype=np.intc)
+        self.x = np.array(out[:, 4:], dtype=np.float64)
+        self.first_index_of_molecule = np.flatnonzero(out[:, 1] == 0).astype(np.intc)
+        self.N_steps_completed = 0

@@ -1,0 +1,90 @@
+"""create_initial_conditions (pyrdsim.pyx:2634-2828): placement on the CPU
+(relaxation off), the relaxed version on the GPU."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import deck_dict, in_deck, load_fixture
+
+
+def _pairwise(y):
+    return np.sqrt(((y[:, None, :] - y[None, :, :]) ** 2).sum(-1))
+
+
+def _patchy_system():
+    from pyrdsim_gb300 import system
+    return system({"seed": 5})
+
+
+def test_reference_molecule_minimises_the_bonded_energy():
+    from pyrdsim_gb300 import initial_conditions as ic
+    fx = load_fixture("patchy")
+    with in_deck(deck_dict(fx)):
+        s = _patchy_system()
+        m = s._model
+        ref = ic.create_reference_molecule(m.molecule_interactions[0], 4, 2,
+                                           np.random.default_rng(1))
+    d = _pairwise(ref)
+    np.testing.assert_allclose(d[0, 1:], 0.5, atol=1e-4)          # core-patch bonds
+    np.testing.assert_allclose(sorted(d[1:, 1:][np.triu_indices(3, 1)]),
+                               [0.5 * np.sqrt(3)] * 3, atol=1e-3)  # 120-degree patches
+    np.testing.assert_array_equal(ref[0], 0.0)
+
+
+def test_placement_follows_the_reference_rules(tmp_path):
+    fx = load_fixture("patchy")
+    with in_deck(deck_dict(fx)):
+        s = _patchy_system()
+        m = s._model
+        out = s.create_initial_conditions({0: 24}, {0: [0, 1, 1, 2]}, relax=False)
+        from pyrdsim_gb300 import decks
+        x, mol, types, first = decks.load_initial_conditions(
+            m.initial_conditions_filename, m.N_dim, m.N_species, tuple(m.comment_chars))
+    assert out.shape == (96, 6)
+    np.testing.assert_array_equal(out[:, 1], np.tile(np.arange(4), 24))
+    np.testing.assert_array_equal(out[:, 0], np.repeat(np.arange(24), 4))
+    np.testing.assert_array_equal(out[:, 3], np.tile([0, 1, 1, 2], 24))
+    L = np.asarray(m.L)
+    assert (out[:, 4:] >= 0).all() and (out[:, 4:] <= L).all()
+    # every molecule is a rigid copy of the first one
+    ref = _pairwise(out[:4, 4:])
+    for k in range(24):
+        np.testing.assert_allclose(_pairwise(out[4 * k:4 * k + 4, 4:]), ref, atol=1e-9)
+    # from the fourth molecule on, first atoms keep rs / 4 from earlier ones
+    c = out[out[:, 1] == 0, 4:]
+    for i in range(3, 24):
+        assert np.sqrt(((c[:i] - c[i]) ** 2).sum(-1)).min() >= m.rs / 4
+    # the initial-condition file holds the same state (5 decimals)
+    np.testing.assert_allclose(x, out[:, 4:], atol=1e-5)
+    np.testing.assert_array_equal(types, out[:, 3])
+    np.testing.assert_array_equal(first, np.arange(0, 96, 4))
+
+
+def test_reference_configuration_files(tmp_path):
+    fx = load_fixture("patchy")
+    good = tmp_path / "ref.txt"
+    np.savetxt(good, [[0, 0], [0.5, 0], [-0.25, 0.433], [-0.25, -0.433]])
+    bad = tmp_path / "bad.txt"
+    np.savetxt(bad, [[0, 0], [0.5, 0]])
+    with in_deck(deck_dict(fx)):
+        s = _patchy_system()
+        out = s.create_initial_conditions({0: 6}, {0: [0, 1, 1, 1]},
+                                          reference_configurations={0: str(good)}, relax=False)
+        np.testing.assert_allclose(_pairwise(out[:4, 4:]), _pairwise(np.loadtxt(good)),
+                                   atol=1e-9)
+        with pytest.raises(RuntimeError, match="has 2 atoms, but interaction parameters"):
+            s.create_initial_conditions({0: 6}, {0: [0, 1, 1, 1]},
+                                        reference_configurations={0: str(bad)}, relax=False)
+
+
+@pytest.mark.gpu
+def test_relaxed_initial_conditions_on_the_gpu():
+    fx = load_fixture("patchy")
+    with in_deck(deck_dict(fx)):
+        s = _patchy_system()
+        m = s._model
+        out = s.create_initial_conditions({0: 12}, {0: [0, 1, 1, 2]})
+        assert np.isfinite(out[:, 4:]).all()
+        assert s._engine.observables()["min_distance"] >= m.rs / 10
+        assert os.path.exists(m.initial_conditions_filename)
