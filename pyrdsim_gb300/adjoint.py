@@ -195,3 +195,43 @@ def trajectory_loss(x0, params, xi, adj):
     if _FN is None:
         _FN = _function()
     return _FN.apply(x0, params, xi, adj)
+
+
+def _main(argv=None):
+    """Loss and gradients of the mixed Lennard-Jones + Yukawa workload:
+    ``python -m pyrdsim_gb300.adjoint --n 16384 --steps 1000``."""
+    import argparse
+    import time
+
+    import torch
+
+    from . import workloads
+    p = argparse.ArgumentParser()
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--loss-steps", type=int, default=0, help="default: half the steps")
+    p.add_argument("--checkpoint-every", type=int, default=32)
+    p.add_argument("--repeat", type=int, default=2)
+    a = p.parse_args(argv)
+    w = workloads.mixed_lj_yukawa(n=a.n)
+    K = a.loss_steps or max(1, a.steps // 2)
+    adj = Adjoint(2, w["L"], w["dt"], w["mobility"], w["types"], workloads.mixed_lj_yukawa_laws(w),
+                  loss_steps=K, checkpoint_every=a.checkpoint_every)
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    xi = torch.randn((a.steps, a.n, 2), dtype=torch.float64, device="cuda", generator=gen)
+    x0 = torch.tensor(w["x0"], dtype=torch.float64, device="cuda")
+    params = workloads.mixed_lj_yukawa_params(w["theta"])
+    for _ in range(a.repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss, _ = adj.forward(x0, params, xi)
+        t1 = time.perf_counter()
+        gx, gp = adj.backward()
+        t2 = time.perf_counter()
+    print(f"N={a.n} T={a.steps} K={K} E={a.checkpoint_every}: loss {loss:.10g}, "
+          f"forward {1e6 * (t1 - t0) / a.steps:.1f} us/step, "
+          f"backward {1e6 * (t2 - t1) / a.steps:.1f} us/step, |dL/dx0| {float(gx.norm()):.6g}")
+
+
+if __name__ == "__main__":
+    _main()
