@@ -120,9 +120,12 @@ struct rdsim_handle {
   ErrDev* err = nullptr;
   double* cl_d = nullptr;
   int cx = 0, cm = 0, co = 0;
-  // host copies of static per-particle data (caller order)
+  // static per-particle data (caller order): host copies and device copies
   std::vector<uint32_t> meta_static;  // local << 16 | template << 24
   std::vector<int> mol_h;
+  uint32_t* meta_static_d = nullptr;
+  int* mol_static_d = nullptr;
+  int* flag_d = nullptr;              // first problem of a state upload
   // injected noise staging
   double *inj_xi = nullptr, *inj_u1 = nullptr, *inj_u2 = nullptr;
   size_t inj_steps = 0;
@@ -441,66 +444,40 @@ int check_device_error(rdsim_handle* h) {
   return fail(e.code, buf);
 }
 
-// float64 -> 64-bit fixed point (host, long double).
-uint64_t to_fixed(double x, double L, bool periodic, long long Si) {
-  if (periodic) {
-    long double f = std::fmod((long double)x, (long double)L);
-    if (f < 0) f += (long double)L;
-    long double v = f / (long double)L * (long double)TWO64;
-    if (v >= (long double)TWO64) v -= (long double)TWO64;
-    if (v < 0) v = 0;
-    long double fl = std::floor(v + 0.5L);
-    if (fl >= (long double)TWO64) fl -= (long double)TWO64;
-    return (uint64_t)fl;
-  }
-  long double v = (long double)x / (long double)L * (long double)Si;
-  long long q = (long long)std::llround(v);
-  return (uint64_t)q;
-}
-
-int upload_state(rdsim_handle* h, const std::vector<double>& x, const std::vector<int>& types) {
-  const int N = h->N, D = h->D;
-  std::vector<uint32_t> hx[3], lx[3];
-  for (int k = 0; k < D; k++) {
-    hx[k].resize(N);
-    lx[k].resize(N);
-  }
-  std::vector<uint32_t> meta(N);
-  std::vector<int> pid(N);
-  for (int s = 0; s < h->nsys; s++) {
-    const HostSys& q = h->hs[s];
-    for (int i = 0; i < q.n; i++) {
-      const int g = q.p0 + i;  // initial slot = caller index
-      for (int k = 0; k < D; k++) {
-        double v = x[(size_t)g * D + k];
-        bool per = (q.periodic_mask >> k) & 1;
-        if (!per) {
-          // int64 fixed point holds [-L, L] (L maps to 2^63 - 2^34)
-          if (!(v >= -q.L[k] && v <= q.L[k] * (1.0 + 1e-9)))
-            return fail(RDSIM_ERR_ARG, "initial position outside the reflecting box");
-        } else if (!std::isfinite(v)) {
-          return fail(RDSIM_ERR_ARG, "non-finite initial position");
-        }
-        uint64_t X = to_fixed(v, q.L[k], per, q.Si[k]);
-        hx[k][g] = (uint32_t)(X >> 32);
-        lx[k][g] = (uint32_t)X;
-      }
-      int t = types[g];
-      if (t < 0 || t >= h->sys_h[s].ntypes)
-        return fail(RDSIM_ERR_ARG, "particle type without tau_by_tauD entry");
-      meta[g] = h->meta_static[g] | (uint32_t)t | ((uint32_t)t << 8);
-      pid[g] = g;
-    }
-  }
+// Caller-order float64 positions and types in xbuf / tbuf (device) -> the
+// engine's state (fixed point, slot = caller index), converted exactly on
+// the device (fixed_from_double).
+int upload_state(rdsim_handle* h) {
+  const int N = h->N;
   h->cx = h->cm = h->co = 0;
-  for (int k = 0; k < D; k++) {
-    CK(cudaMemcpyAsync(h->xh[0][k], hx[k].data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->xl[0][k], lx[k].data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemsetAsync(h->flag_d, 0, sizeof(int), h->stream));
+  StateOut a;
+  std::memset(&a, 0, sizeof a);
+  for (int k = 0; k < 3; k++) {
+    a.xh[k] = h->xh[0][k];
+    a.xl[k] = h->xl[0][k];
   }
-  CK(cudaMemcpyAsync(h->meta[0], meta.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
-  CK(cudaMemcpyAsync(h->mol[0], h->mol_h.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
-  CK(cudaMemcpyAsync(h->pid[0], pid.data(), 4 * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  a.meta = h->meta[0];
+  a.mol = h->mol[0];
+  a.pid = h->pid[0];
+  a.n = N;
+  const unsigned g = nblk(N);
+  if (h->D == 2)
+    k_from_double<2><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, h->xbuf, h->tbuf, h->meta_static_d,
+                                               h->mol_static_d, a, h->flag_d);
+  else if (h->D == 3)
+    k_from_double<3><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, h->xbuf, h->tbuf, h->meta_static_d,
+                                               h->mol_static_d, a, h->flag_d);
+  else
+    k_from_double<1><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, h->xbuf, h->tbuf, h->meta_static_d,
+                                               h->mol_static_d, a, h->flag_d);
+  CK(cudaGetLastError());
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, h->flag_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  if (bad == 1) return fail(RDSIM_ERR_ARG, "initial position outside the reflecting box");
+  if (bad == 2) return fail(RDSIM_ERR_ARG, "non-finite initial position");
+  if (bad == 3) return fail(RDSIM_ERR_ARG, "particle type without tau_by_tauD entry");
   return 0;
 }
 
@@ -587,6 +564,7 @@ void free_all(rdsim_handle* h) {
   }
   for (int k = 0; k < 3; k++) { F(h->xr[k]); F(h->drift[k]); }
   F(h->rates); F(h->xbuf); F(h->tbuf); F(h->err); F(h->cl_d);
+  F(h->meta_static_d); F(h->mol_static_d); F(h->flag_d);
   F(h->inj_xi); F(h->inj_u1); F(h->inj_u2); F(h->traj_x); F(h->traj_t);
   F(h->olaws_d); F(h->owalls_d); F(h->oterms_d); F(h->obs_part); F(h->obs_counts);
   F(h->rdf_counts);
@@ -1153,6 +1131,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = dalloc(&h->rates, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->xbuf, (size_t)N * D, &B))) return bail(rc);
   if ((rc = dalloc(&h->tbuf, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->meta_static_d, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->mol_static_d, N, &B))) return bail(rc);
+  if ((rc = dalloc(&h->flag_d, 1, &B))) return bail(rc);
   if ((rc = dalloc(&h->err, 1, &B))) return bail(rc);
   if ((rc = dalloc(&h->step_dev, 1, &B))) return bail(rc);
   {
@@ -1193,7 +1174,11 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   for (int k = 0; k < D; k++)
     if (cudaMemsetAsync(h->drift[k], 0, sizeof(float) * N, h->stream) != cudaSuccess)
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
-  if ((rc = upload_state(h, x_all, t_all))) return bail(rc);
+  if ((rc = up(h->meta_static_d, h->meta_static.data(), sizeof(uint32_t) * (size_t)N))) return bail(rc);
+  if ((rc = up(h->mol_static_d, h->mol_h.data(), sizeof(int) * (size_t)N))) return bail(rc);
+  if ((rc = up(h->xbuf, x_all.data(), sizeof(double) * x_all.size()))) return bail(rc);
+  if ((rc = up(h->tbuf, t_all.data(), sizeof(int) * t_all.size()))) return bail(rc);
+  if ((rc = upload_state(h))) return bail(rc);
   if ((rc = initial_drift(h))) return bail(rc);
   *out = h;
   return 0;
@@ -1295,15 +1280,18 @@ int rdsim_set_state(rdsim_handle* h, const double* x, const int32_t* types) {
   if (!h) return fail(RDSIM_ERR_ARG, "null handle");
   CK(cudaSetDevice(h->device));
   const int N = h->N, D = h->D;
-  std::vector<double> xv((size_t)N * D);
-  std::vector<int> tv(N);
   if (!x || !types) {
-    int rc = rdsim_get_state(h, x ? nullptr : xv.data(), types ? nullptr : tv.data());
-    if (rc) return rc;
+    // the part not given: the current state, in caller order, on the device
+    Args a = make_args(h);
+    const unsigned g = nblk(N);
+    if (D == 2) k_to_double<2><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, h->xbuf, h->tbuf);
+    else if (D == 3) k_to_double<3><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, h->xbuf, h->tbuf);
+    else k_to_double<1><<<g, 256, 0, h->stream>>>(h->sys_d, h->sid, a, h->xbuf, h->tbuf);
+    CK(cudaGetLastError());
   }
-  if (x) std::memcpy(xv.data(), x, sizeof(double) * (size_t)N * D);
-  if (types) std::memcpy(tv.data(), types, sizeof(int) * (size_t)N);
-  int rc = upload_state(h, xv, tv);
+  if (x) CK(cudaMemcpyAsync(h->xbuf, x, sizeof(double) * (size_t)N * D, cudaMemcpyHostToDevice, h->stream));
+  if (types) CK(cudaMemcpyAsync(h->tbuf, types, sizeof(int) * (size_t)N, cudaMemcpyHostToDevice, h->stream));
+  int rc = upload_state(h);
   if (rc) return rc;
   return initial_drift(h);
 }

@@ -64,6 +64,73 @@ __device__ inline double fixed_to_double(const SysDev& s, int k, uint32_t h, uin
   return __dmul_rn(__ll2double_rn((long long)X), s.unit_d[k]);
 }
 
+// Binary significand and exponent of a finite non-zero double: |v| = m 2^e
+// with m in [2^52, 2^53).
+__host__ __device__ inline unsigned long long significand(double v, int* e) {
+  int ex = 0;
+  const double f = frexp(fabs(v), &ex);
+  *e = ex - 53;
+  return (unsigned long long)ldexp(f, 53);
+}
+
+// float64 -> 64-bit fixed point, exactly: periodic dimensions give
+// round(frac(x / L) * 2^64) mod 2^64 (x taken modulo L; halves round up),
+// reflecting ones llround(x / L * Si).  128-bit integer arithmetic on the
+// significands, so every host and the device give the same value.  False
+// for a non-finite x.
+__host__ __device__ inline bool fixed_from_double(double x, double L, bool periodic,
+                                                  long long Si, unsigned long long* out) {
+  typedef unsigned __int128 u128;
+  if (!(x - x == 0.0)) return false;  // inf or nan
+  int eL = 0;
+  const u128 mL = significand(L, &eL);
+  if (periodic) {
+    const double f = fmod(x, L);  // exact, |f| < L, the sign of x
+    if (f == 0.0) {
+      *out = 0ull;
+      return true;
+    }
+    int ef = 0;
+    const u128 mf = significand(f, &ef);
+    // y = |f| 2^64 / L = mf 2^s / mL with s <= 64 (|f| < L)
+    const int sh = ef + 64 - eL;
+    u128 N = 0, Dn = 1;
+    if (sh >= 0) {
+      N = mf << sh;
+      Dn = mL;
+    } else if (-sh < 70) {
+      N = mf;
+      Dn = mL << (-sh);
+    }
+    // f >= 0: floor(y + 1/2); f < 0: 2^64 - ceil(y - 1/2)
+    const bool neg = f < 0.0;
+    const u128 q = neg ? (2 * N + Dn - 1) / (2 * Dn) : (2 * N + Dn) / (2 * Dn);
+    const unsigned long long X = (unsigned long long)q;
+    *out = neg ? 0ull - X : X;
+    return true;
+  }
+  if (x == 0.0) {
+    *out = 0ull;
+    return true;
+  }
+  int ea = 0;
+  const u128 ma = significand(x, &ea);
+  // y = |x| Si / L = ma Si 2^s / mL with s <= 1 (|x| <= L (1 + 1e-9))
+  const int sh = ea - eL;
+  const u128 N0 = ma * (u128)(unsigned long long)Si;
+  u128 N = 0, Dn = 1;
+  if (sh >= 0) {
+    N = N0 << sh;
+    Dn = mL;
+  } else if (-sh < 74) {
+    N = N0;
+    Dn = mL << (-sh);
+  }
+  const long long q = (long long)((2 * N + Dn) / (2 * Dn));  // half away from zero
+  *out = (unsigned long long)(x < 0.0 ? -q : q);
+  return true;
+}
+
 // Distance of two particles exactly as pyrdsim.pyx:1619-1633 computes it
 // (float64, C round() minimum image, pow(v, 2) summed in dimension order).
 template <int D>
@@ -797,6 +864,54 @@ __global__ void k_to_double(const SysDev* sysv, const int* sid, Args a, double* 
 #pragma unroll
   for (int k = 0; k < D; k++) x[(size_t)pid * D + k] = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
   if (types) types[pid] = a.meta[gi] & 0xff;
+}
+
+// State upload: caller-order float64 positions x and types -> the fixed-point
+// arrays (slot = caller index), meta and molecule words.  bad receives the
+// first problem: 1 reflecting position outside [-L, L], 2 non-finite
+// position, 3 type without a tau_by_tauD entry.
+struct StateOut {
+  uint32_t* xh[3];
+  uint32_t* xl[3];
+  uint32_t* meta;
+  int* mol;
+  int* pid;
+  int n;
+};
+
+template <int D>
+__global__ void k_from_double(const SysDev* sysv, const int* sid, const double* x,
+                              const int* types, const uint32_t* meta_static,
+                              const int* mol_static, StateOut a, int* bad) {
+  pdl_trigger();
+  pdl_wait();
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= a.n) return;
+  const SysDev& s = sysv[sid[gi]];
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    const double v = x[(size_t)gi * D + k];
+    const bool per = (s.periodic >> k) & 1;
+    if (!per && !(v >= -s.L[k] && v <= s.L[k] * (1.0 + 1e-9))) {
+      atomicCAS(bad, 0, 1);
+      return;
+    }
+    unsigned long long X = 0;
+    if (!fixed_from_double(v, s.L[k], per, s.Si[k], &X)) {
+      atomicCAS(bad, 0, 2);
+      return;
+    }
+    a.xh[k][gi] = (uint32_t)(X >> 32);
+    a.xl[k][gi] = (uint32_t)X;
+  }
+  const int t = types[gi];
+  if (t < 0 || t >= s.ntypes) {
+    atomicCAS(bad, 0, 3);
+    return;
+  }
+  a.meta[gi] = meta_static[gi] | (uint32_t)t | ((uint32_t)t << 8);
+  a.mol[gi] = mol_static[gi];
+  a.pid[gi] = gi;
 }
 
 // trajectory frame: positions (float64) and types in caller order

@@ -174,9 +174,15 @@ class Engine:
         t = None if types is None else np.ascontiguousarray(types, dtype=np.int32)
         _check(self.lib.rdsim_set_state(self.h, abi.dptr(x), abi.iptr(t)))
 
-    def state(self):
-        x = np.empty((self.N, self.D))
-        t = np.empty(self.N, dtype=np.int32)
+    def state(self, x=None, t=None):
+        """Positions [N, D] and types [N]; ``x`` / ``t`` may be preallocated
+        (e.g. pinned) C-contiguous float64 / int32 arrays to fill."""
+        x = np.empty((self.N, self.D)) if x is None else x
+        t = np.empty(self.N, dtype=np.int32) if t is None else t
+        if x.shape != (self.N, self.D) or x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise ValueError("x must be a C-contiguous float64 array of shape (N, D)")
+        if t.shape != (self.N,) or t.dtype != np.int32 or not t.flags.c_contiguous:
+            raise ValueError("t must be a C-contiguous int32 array of shape (N,)")
         _check(self.lib.rdsim_get_state(self.h, abi.dptr(x), abi.iptr(t)))
         return x, t
 

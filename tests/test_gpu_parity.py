@@ -315,3 +315,36 @@ def test_inhibited_reactions_at_scale():
     r = orc.reaction_rates(recompute=True)
     np.testing.assert_array_equal(eng.reaction_rates(), r)
     assert (r == 0).any() and (r == 25.0).any() and (r == 10.0).any()
+
+
+def test_state_upload_is_exact_and_idempotent():
+    """Positions are converted to 64-bit fixed point exactly (128-bit integer
+    arithmetic on the device): a second round trip through set_state /
+    get_state returns the same doubles, periodic L/2 and -L/4 land on
+    2^63 and 3 * 2^62 units, and every coordinate moves by at most one unit
+    (and the float64 rounding of the read-back)."""
+    fx, sd = _case("two_species_wall_rx")
+    eng = _engine([sd])
+    m = sd.model
+    rng = np.random.default_rng(5)
+    n = sd.n_particles
+    L = np.asarray(m.L, dtype=float)
+    x = rng.random((n, 2)) * L
+    x[0, 0] = L[0] / 2
+    x[1, 0] = -L[0] / 4
+    t = eng.state()[1]
+    eng.set_state(x, t)
+    x1, _ = eng.state()
+    eng.set_state(x1, t)
+    x2, _ = eng.state()
+    np.testing.assert_array_equal(x1, x2)
+    unit = np.where(np.asarray(m.periodic) > 0, L / 2.0 ** 64, L / (2.0 ** 63 - 2.0 ** 34))
+    ref = x.copy()
+    ref[1, 0] += L[0]
+    # one fixed-point unit, plus the rounding of the float64 read-back
+    assert (np.abs(x1 - ref) <= unit * 1.0001 + np.spacing(np.abs(ref))).all()
+    assert x1[0, 0] == L[0] / 2 and x1[1, 0] == 0.75 * L[0]
+    with pytest.raises(RuntimeError):
+        bad = x.copy()
+        bad[2, 1] = 2 * L[1]  # outside the reflecting box
+        eng.set_state(bad, t)
