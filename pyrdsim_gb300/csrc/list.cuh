@@ -708,14 +708,21 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
     lr.store(reinterpret_cast<int*>(rx1), nr);
   }
   pdl_wait();
+  // the step counter, both parities' counts and this warp's first record of
+  // each parity are loaded together (one round trip instead of three)
+  const int w0 = (int)((blockIdx.x * LBLOCK + threadIdx.x) >> 5);
+  const int n0 = a.rx_count[0], n1 = a.rx_count[1];
+  const int4 zero = make_int4(0, 0, 0, 0);
+  const int4 f0 = w0 < a.npad ? a.rx_list[w0] : zero;
+  const int4 f1 = w0 < a.npad ? a.rx_list[(size_t)a.npad + w0] : zero;
   const int p = (int)(eff_step(a) & 1);
-  const int n = a.rx_count[p];
+  const int n = p ? n1 : n0;
   __syncthreads();
   const int4* list = a.rx_list + (size_t)p * a.npad;
   const int lane = threadIdx.x & 31;
   const int nwarps = (int)(gridDim.x * LBLOCK / 32);
-  for (int q = (int)((blockIdx.x * LBLOCK + threadIdx.x) >> 5); q < n; q += nwarps) {
-    const int4 rec = list[q];
+  for (int q = w0; q < n; q += nwarps) {
+    const int4 rec = q == w0 ? (p ? f1 : f0) : list[q];
     const int m = rec.x, cnt = rec.z, pid = rec.w;
     const uint32_t mm = (uint32_t)rec.y;
     const SysDev& s = a.single ? sys1 : a.sys[a.sid[m]];
