@@ -70,6 +70,11 @@ int rdsim_adjoint_forward(rdsim_adjoint* h, const double* x0, const double* para
 int rdsim_adjoint_backward(rdsim_adjoint* h, double dloss, double* grad_x0,
                            double* grad_params);
 
+/* Neighbour lists of the last forward pass: each served *states_per_list
+ * consecutive states (8, 4 or 2 when checkpoint_every allows it and no
+ * particle outran the skin, else 1); *list_width entries per lane. */
+int rdsim_adjoint_get_lists(rdsim_adjoint* h, int32_t* states_per_list, int32_t* list_width);
+
 /* CUDA stream of the handle (cudaStream_t). */
 int rdsim_adjoint_get_stream(rdsim_adjoint* h, void** stream);
 

@@ -24,7 +24,7 @@ from . import abi
 from .engine import EngineError, load_library
 
 EXPORTS = ["rdsim_adjoint_create", "rdsim_adjoint_destroy", "rdsim_adjoint_forward",
-           "rdsim_adjoint_backward", "rdsim_adjoint_get_stream"]
+           "rdsim_adjoint_backward", "rdsim_adjoint_get_lists", "rdsim_adjoint_get_stream"]
 
 MAX_LAWS = 8
 
@@ -48,6 +48,7 @@ def _lib():
         L.rdsim_adjoint_forward.argtypes = [vp, vp, dp, vp, C.c_int32, dp, vp]
         L.rdsim_adjoint_backward.argtypes = [vp, C.c_double, vp, dp]
         L.rdsim_adjoint_get_stream.argtypes = [vp, C.POINTER(vp)]
+        L.rdsim_adjoint_get_lists.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L._adjoint_declared = True
     return L
 
@@ -114,6 +115,13 @@ class Adjoint:
             self.close()
         except Exception:
             pass
+
+    @property
+    def states_per_list(self):
+        """States each neighbour list served in the last forward pass."""
+        r, w = C.c_int32(), C.c_int32()
+        _check(self.lib.rdsim_adjoint_get_lists(self.h, C.byref(r), C.byref(w)))
+        return r.value
 
     def initial_params(self):
         """(u0, r0) of every law as given at construction, [n_laws, 2]."""

@@ -62,7 +62,9 @@ struct AdjArgs {
   int nc[3], ncell;
   double L[3], cellinv[3];
   float Lf[3], Linvf[3];
-  float cut2f;                  // float32 screen: above the largest rc^2
+  double rc2max;                // largest law cutoff^2: list entries beyond skip
+  float cut2f;                  // float32 screen of the list in use
+  float move2f;                 // displacement^2 allowed while a list is reused                  // float32 screen: above the largest rc^2
   double c[MAXT], s[MAXT];      // dt D and sqrt(2 dt D) per type
   double wU, wW;                // loss weights 1/K and 1/(K d V)
   unsigned char lawmask[MAXT * MAXT];  // bit l: law l applies to (ti, tj)
@@ -216,7 +218,8 @@ __global__ void k_cell_sort(int ncell, const double* __restrict__ x,
   count[c] = 0;
 }
 
-// Neighbour list of one state.  TPP lanes per particle i: lane l takes the
+// Neighbour list of one state (or of R states: the screen distance then
+// includes twice the allowed displacement).  TPP lanes per particle i: lane l takes the
 // members l, l + TPP, ... of each of the 3^D cells around i's cell (cells in
 // a fixed order, members in index order) that pass the float32 distance
 // screen and keeps them in its own sub-list nbr[(e * TPP + l) * N + i],
@@ -228,7 +231,8 @@ __global__ void __launch_bounds__(BLK) k_adj_list(AdjArgs g, const double* __res
                                                   const int* __restrict__ idx,
                                                   const float* __restrict__ xs, int W,
                                                   int* __restrict__ nbr, int* __restrict__ ncnt,
-                                                  int* __restrict__ maxcnt) {
+                                                  int* __restrict__ maxcnt,
+                                                  float* __restrict__ xr) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = t % TPP, i = t / TPP;
   int cnt = 0;
@@ -278,6 +282,10 @@ __global__ void __launch_bounds__(BLK) k_adj_list(AdjArgs g, const double* __res
           }
         }
     ncnt[(size_t)lane * g.N + i] = cnt;
+    if (xr && lane == 0) {  // positions of this list, for the displacement check
+#pragma unroll
+      for (int k = 0; k < D; k++) xr[(size_t)i * D + k] = xf[k];
+    }
   }
   const int m = __reduce_max_sync(0xffffffffu, cnt);
   if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(maxcnt, m);
@@ -321,7 +329,9 @@ __global__ void __launch_bounds__(BLK) k_adj_step(AdjArgs g, const double* __res
                                                   const int* __restrict__ types,
                                                   const double* __restrict__ noise,
                                                   double* __restrict__ x_out,
-                                                  double* __restrict__ lacc) {
+                                                  double* __restrict__ lacc,
+                                                  const float* __restrict__ xr,
+                                                  int* __restrict__ moved) {
   __shared__ Law slaws[MAXL];
   if (threadIdx.x < (unsigned)g.nlaws) slaws[threadIdx.x] = g.laws[threadIdx.x];
   __syncthreads();
@@ -342,6 +352,7 @@ __global__ void __launch_bounds__(BLK) k_adj_step(AdjArgs g, const double* __res
     double r2 = 0.0;
 #pragma unroll
     for (int k = 0; k < D; k++) r2 += d[k] * d[k];
+    if (!(r2 < g.rc2max)) return;  // in the list's skin only
     const double ir = rsqrt(r2), r = r2 * ir;
     // iteration q takes each lane's q-th law: lanes of different type
     // pairs evaluate their first laws together
@@ -360,6 +371,18 @@ __global__ void __launch_bounds__(BLK) k_adj_step(AdjArgs g, const double* __res
   for (int k = 0; k < D; k++) a[k] = lane_sum(a[k]);
   if (FL & F_LOSS) loss = lane_sum(loss);
   if (!own || lane != 0) return;
+  if (xr) {
+    // the list in use dates from an earlier state: it holds every pair in
+    // range only while no particle has moved more than the skin allows
+    float d2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      float v = (float)xi[k] - xr[(size_t)i * D + k];
+      v -= g.Lf[k] * rintf(v * g.Linvf[k]);
+      d2 += v * v;
+    }
+    if (d2 > g.move2f) atomicOr(moved, 1);
+  }
   if (FL & F_LOSS) lacc[i] += loss;
   if (FL & F_STEP) {
 #pragma unroll
@@ -407,6 +430,7 @@ __global__ void __launch_bounds__(BLK) k_adj_back(AdjArgs g, const double* __res
     double r2 = 0.0;
 #pragma unroll
     for (int k = 0; k < D; k++) r2 += d[k] * d[k];
+    if (!(r2 < g.rc2max)) return;  // in the list's skin only
     const double ir = rsqrt(r2), r = r2 * ir;
     double rh[3] = {0.0, 0.0, 0.0}, dw[3] = {0.0, 0.0, 0.0};
     double rdw = 0.0;  // rhat . (w_j - w_i)
@@ -508,6 +532,12 @@ struct rdsim_adjoint {
   int W = 0;
   int *seg_nbr = nullptr, *seg_ncnt = nullptr;
   int* maxcnt = nullptr;
+  // list reuse: one list serves R consecutive states (R divides E) when no
+  // particle moves more than the skin allows in between
+  int R = 1, R_used = 1;
+  float cut2f_exact = 0.f, cut2f_skin = 0.f;
+  float* xr = nullptr;             // [N][D] float32 positions of the forward list
+  int* moved = nullptr;
   double* seg_x = nullptr;         // [E][N][D] states of the current segment
   double* ckpt = nullptr;          // [nckpt][N][D] states 0, E, 2E, ...
   size_t ckpt_cap = 0;
@@ -527,7 +557,7 @@ void free_adj(rdsim_adjoint* h) {
     if (p) cudaFree(p);
   };
   F(h->types); F(h->count); F(h->cursor); F(h->start); F(h->idx); F(h->xs);
-  F(h->seg_nbr); F(h->seg_ncnt); F(h->maxcnt); F(h->seg_x);
+  F(h->seg_nbr); F(h->seg_ncnt); F(h->maxcnt); F(h->seg_x); F(h->xr); F(h->moved);
   F(h->ckpt); F(h->xT); F(h->lacc); F(h->lam[0]); F(h->lam[1]); F(h->gpart); F(h->red);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
@@ -548,7 +578,7 @@ int alloc_lists(rdsim_adjoint* h, int W) {
 }
 
 template <int D>
-void build_list_d(rdsim_adjoint* h, const double* x, int slot) {
+void build_list_d(rdsim_adjoint* h, const double* x, int slot, float* xr) {
   const AdjArgs& g = h->g;
   k_bin<D><<<nblk(g.N), BLK, 0, h->stream>>>(g, x, h->count);
   k_scan<<<1, SCAN_T, 0, h->stream>>>(h->count, g.ncell, h->start, h->cursor);
@@ -557,36 +587,40 @@ void build_list_d(rdsim_adjoint* h, const double* x, int slot) {
                                                         h->count);
   k_adj_list<D><<<pblk(g.N), BLK, 0, h->stream>>>(g, x, h->start, h->idx, h->xs, h->W,
                                                    slot_nbr(h, slot), slot_ncnt(h, slot),
-                                                   h->maxcnt);
+                                                   h->maxcnt, xr);
 }
 
-// Cells and neighbour list of state x into list slot `slot`.
-void build_list(rdsim_adjoint* h, const double* x, int slot) {
-  if (h->g.D == 2) build_list_d<2>(h, x, slot);
-  else if (h->g.D == 3) build_list_d<3>(h, x, slot);
-  else build_list_d<1>(h, x, slot);
+// Cells and neighbour list of state x into list slot `slot` (and its float32
+// positions into xr when given).
+void build_list(rdsim_adjoint* h, const double* x, int slot, float* xr = nullptr) {
+  if (h->g.D == 2) build_list_d<2>(h, x, slot, xr);
+  else if (h->g.D == 3) build_list_d<3>(h, x, slot, xr);
+  else build_list_d<1>(h, x, slot, xr);
 }
 
 template <int D, int FL>
-void step_k(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out) {
+void step_k(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out,
+            const float* xr) {
   k_adj_step<D, FL><<<pblk(h->g.N), BLK, 0, h->stream>>>(h->g, x, slot_nbr(h, slot),
                                                           slot_ncnt(h, slot), h->W, h->types,
-                                                          noise, x_out, h->lacc);
+                                                          noise, x_out, h->lacc, xr, h->moved);
 }
 
 template <int D>
 void step_d(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out,
-            int flags) {
-  if (flags == F_STEP) step_k<D, F_STEP>(h, x, slot, noise, x_out);
-  else if (flags == F_LOSS) step_k<D, F_LOSS>(h, x, slot, noise, x_out);
-  else step_k<D, F_STEP | F_LOSS>(h, x, slot, noise, x_out);
+            int flags, const float* xr) {
+  if (flags == F_STEP) step_k<D, F_STEP>(h, x, slot, noise, x_out, xr);
+  else if (flags == F_LOSS) step_k<D, F_LOSS>(h, x, slot, noise, x_out, xr);
+  else step_k<D, F_STEP | F_LOSS>(h, x, slot, noise, x_out, xr);
 }
 
+// One state's kernel (loss terms and/or the step); with xr the displacement
+// since the list was built is checked.
 void step(rdsim_adjoint* h, const double* x, int slot, const double* noise, double* x_out,
-          int flags) {
-  if (h->g.D == 2) step_d<2>(h, x, slot, noise, x_out, flags);
-  else if (h->g.D == 3) step_d<3>(h, x, slot, noise, x_out, flags);
-  else step_d<1>(h, x, slot, noise, x_out, flags);
+          int flags, const float* xr = nullptr) {
+  if (h->g.D == 2) step_d<2>(h, x, slot, noise, x_out, flags, xr);
+  else if (h->g.D == 3) step_d<3>(h, x, slot, noise, x_out, flags, xr);
+  else step_d<1>(h, x, slot, noise, x_out, flags, xr);
 }
 
 template <int D, int FL>
@@ -632,6 +666,16 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
   g.D = D;
   g.nlaws = s->n_laws;
   double rc_max = 0.0, V = 1.0;
+  h->E = s->checkpoint_every;
+  // list reuse: R states per list (R divides E); the skin covers five
+  // standard deviations of R diffusion steps of the most mobile type per
+  // dimension (a particle that moves farther makes the forward pass repeat
+  // itself with one list per state)
+  double sig = 0.0;
+  for (int t = 0; t < s->n_types; t++)
+    if (s->mobility[t] > 0) sig = std::max(sig, std::sqrt(2.0 * s->dt * s->mobility[t]));
+  h->R = h->E % 8 == 0 ? 8 : (h->E % 4 == 0 ? 4 : (h->E % 2 == 0 ? 2 : 1));
+  const double skin_half = std::max(0.05, 5.0 * sig * std::sqrt((double)h->R) * std::sqrt((double)D));
   for (int l = 0; l < s->n_laws; l++) {
     const rdsim_interaction& it = s->laws[l];
     if (it.law != RDSIM_LAW_LJ && it.law != RDSIM_LAW_YUKAWA) {
@@ -648,12 +692,30 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
     rc_max = std::max(rc_max, it.rc);
     h->laws.push_back(it);
   }
+  double Lmin = 1e300, Lmax = 0.0;
+  for (int k = 0; k < D; k++) {
+    Lmin = std::min(Lmin, s->L[k]);
+    Lmax = std::max(Lmax, s->L[k]);
+  }
+  // screen distances: float32 positions and minimum image err by a few
+  // 1e-7 L per coordinate
+  const double cut_exact = rc_max + 1e-3 + 1e-6 * Lmax;
+  const double cut_skin = cut_exact + 2.0 * skin_half;
+  if (rc_max <= 0 || 2.0 * cut_skin > Lmin) h->R = 1;
+  const double cut_cells = h->R > 1 ? cut_skin : cut_exact;
+  g.rc2max = rc_max * rc_max;
+  h->cut2f_exact = (float)(cut_exact * cut_exact * (1.0 + 1e-6));
+  h->cut2f_skin = (float)(cut_skin * cut_skin * (1.0 + 1e-6));
+  {
+    const double mv = skin_half - 1e-4 - 1e-6 * Lmax;  // float32 check, conservative
+    g.move2f = (float)(mv > 0 ? mv * mv : 0.0);
+  }
   for (int k = 0; k < D; k++) {
     if (!(s->L[k] >= 2.0 * rc_max) || !(s->L[k] > 0)) {
       delete h;
       return fail(RDSIM_ERR_ARG, "box length below twice the largest cutoff");
     }
-    int nc = rc_max > 0 ? (int)std::floor(s->L[k] / rc_max) : 1;
+    int nc = rc_max > 0 ? (int)std::floor(s->L[k] / cut_cells) : 1;
     nc = std::min(std::max(nc, 1), 1 << 12);
     if (nc < 3) nc = 1;
     g.nc[k] = nc;
@@ -664,14 +726,7 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
     V *= s->L[k];
   }
   for (int k = D; k < 3; k++) g.nc[k] = 1;
-  {
-    // float32 screen of candidate pairs: float32 positions and minimum image
-    // err by a few 1e-7 L per coordinate
-    double Lmax = 0.0;
-    for (int k = 0; k < D; k++) Lmax = std::max(Lmax, s->L[k]);
-    const double cut = rc_max + 1e-3 + 1e-6 * Lmax;
-    g.cut2f = (float)(cut * cut * (1.0 + 1e-6));
-  }
+  g.cut2f = h->R > 1 ? h->cut2f_skin : h->cut2f_exact;
   g.ncell = g.nc[0] * g.nc[1] * g.nc[2];
   for (int t = 0; t < s->n_types; t++) {
     const double Dt = s->mobility[t];
@@ -679,7 +734,6 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
     g.s[t] = Dt > 0 ? std::sqrt(2.0 * s->dt * Dt) : 0.0;
   }
   h->K = s->loss_steps;
-  h->E = s->checkpoint_every;
   g.wU = 1.0 / h->K;
   g.wW = 1.0 / (h->K * D * V);
   std::vector<int> types(s->types, s->types + N);
@@ -707,6 +761,8 @@ int rdsim_adjoint_create(const rdsim_adjoint_system* s, int32_t device, rdsim_ad
             cudaMalloc(&h->xs, sizeof(float) * nd) == cudaSuccess &&
             cudaMalloc(&h->seg_ncnt, sizeof(int) * slots * TPP * N) == cudaSuccess &&
             cudaMalloc(&h->maxcnt, sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&h->xr, sizeof(float) * nd) == cudaSuccess &&
+            cudaMalloc(&h->moved, sizeof(int)) == cudaSuccess &&
             cudaMalloc(&h->seg_x, sizeof(double) * h->E * nd) == cudaSuccess &&
             cudaMalloc(&h->xT, sizeof(double) * nd) == cudaSuccess &&
             cudaMalloc(&h->lacc, sizeof(double) * N) == cudaSuccess &&
@@ -740,6 +796,13 @@ int rdsim_adjoint_destroy(rdsim_adjoint* h) {
   cudaSetDevice(h->device);
   free_adj(h);
   delete h;
+  return 0;
+}
+
+int rdsim_adjoint_get_lists(rdsim_adjoint* h, int32_t* states_per_list, int32_t* list_width) {
+  if (!h || !states_per_list || !list_width) return fail(RDSIM_ERR_ARG, "null argument");
+  *states_per_list = h->R_used;
+  *list_width = h->W;
   return 0;
 }
 
@@ -783,9 +846,12 @@ int rdsim_adjoint_forward(rdsim_adjoint* h, const double* x0, const double* para
     h->ckpt_cap = nck * nd;
   }
   const double* cur = nullptr;
+  int R = h->R;
   for (int attempt = 0;; attempt++) {
+    g.cut2f = R > 1 ? h->cut2f_skin : h->cut2f_exact;
     CK(cudaMemsetAsync(h->lacc, 0, sizeof(double) * N, h->stream));
     CK(cudaMemsetAsync(h->maxcnt, 0, sizeof(int), h->stream));
+    CK(cudaMemsetAsync(h->moved, 0, sizeof(int), h->stream));
     CK(cudaMemcpyAsync(h->ckpt, x0, sizeof(double) * nd, cudaMemcpyDeviceToDevice, h->stream));
     // states between checkpoints alternate between seg_x[0] and seg_x[1]
     // (the segment buffer is free during the forward pass; E >= 2 there)
@@ -799,20 +865,27 @@ int rdsim_adjoint_forward(rdsim_adjoint* h, const double* x0, const double* para
         const int m = n + 1;
         nxt = m % E == 0 ? h->ckpt + (size_t)(m / E) * nd : h->seg_x + (size_t)(m & 1) * nd;
       }
-      build_list(h, cur, slot);
-      step(h, cur, slot, n < n_steps ? xi + (size_t)n * nd : nullptr, nxt, flags);
+      if (n % R == 0) build_list(h, cur, slot, R > 1 ? h->xr : nullptr);
+      step(h, cur, slot, n < n_steps ? xi + (size_t)n * nd : nullptr, nxt, flags,
+           R > 1 ? h->xr : nullptr);
       if (nxt) cur = nxt;
     }
     CK(cudaGetLastError());
-    int mx = 0;
+    int mx = 0, moved = 0;
     CK(cudaMemcpyAsync(&mx, h->maxcnt, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(&moved, h->moved, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    if (mx <= h->W) break;
-    // a list row overflowed: widen the lists and run the pass again
-    if (attempt > 0) return fail(RDSIM_ERR_CAPACITY, "neighbour list overflow");
-    int rc = alloc_lists(h, std::min(N, mx + mx / 4 + 4));
-    if (rc) return rc;
+    if (mx <= h->W && !moved) break;
+    if (attempt > 2) return fail(RDSIM_ERR_CAPACITY, "neighbour list overflow");
+    if (moved) {
+      R = 1;  // a particle outran the skin: one list per state
+    } else {
+      // a list row overflowed: widen the lists and run the pass again
+      int rc = alloc_lists(h, std::min(N, mx + mx / 4 + 4));
+      if (rc) return rc;
+    }
   }
+  h->R_used = R;
   if (cur != h->xT) CK(cudaMemcpyAsync(h->xT, cur, sizeof(double) * nd, cudaMemcpyDeviceToDevice, h->stream));
   k_sum_rows<<<1, BLK, 0, h->stream>>>(h->lacc, N, 1, h->red);
   CK(cudaMemcpyAsync(loss, h->red, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -827,38 +900,53 @@ int rdsim_adjoint_backward(rdsim_adjoint* h, double dloss, double* grad_x0, doub
   if (!h || !grad_x0 || !grad_params) return fail(RDSIM_ERR_ARG, "null argument");
   if (h->T < 0) return fail(RDSIM_ERR_ARG, "no forward pass to differentiate");
   CK(cudaSetDevice(h->device));
-  const AdjArgs& g = h->g;
+  AdjArgs& g = h->g;
   const int N = g.N, D = g.D, E = h->E, T = h->T;
   const size_t nd = (size_t)N * D;
   CK(cudaMemsetAsync(h->gpart, 0, sizeof(double) * pblk(N) * NG, h->stream));
   CK(cudaMemsetAsync(h->lam[0], 0, sizeof(double) * nd, h->stream));
+  const int R = h->R_used;
+  g.cut2f = R > 1 ? h->cut2f_skin : h->cut2f_exact;
+  const int extra = E;  // list slot of the final state when it starts a list
   int cur = 0;     // lam[cur] holds lambda_{n+1}
   int seg = -1;    // base step of the states held in seg_x
+  // states b .. b + E - 1 below T recomputed from checkpoint b / E, with the
+  // lists of states b, b + R, ... in slots 0, 1, ... (the forward pass used
+  // the list of state floor(n / R) R for state n; R divides E)
+  auto segment = [&](int b) -> int {
+    if (b == seg) return 0;
+    CK(cudaMemcpyAsync(h->seg_x, h->ckpt + (size_t)(b / E) * nd, sizeof(double) * nd,
+                       cudaMemcpyDeviceToDevice, h->stream));
+    const int last = std::min(b + E - 1, T - 1);
+    for (int q = 0; q <= last - b; q++) {
+      double* xq = h->seg_x + (size_t)q * nd;
+      if (q > 0) step(h, xq - nd, (q - 1) / R, h->xi + (size_t)(b + q - 1) * nd, xq, F_STEP);
+      if (q % R == 0) build_list(h, xq, q / R);
+    }
+    seg = b;
+    return 0;
+  };
   for (int n = T; n >= 0; n--) {
     const double* x;
     int slot;
     if (n == T) {
       x = h->xT;
-      slot = E;
-      build_list(h, x, slot);
+      const int r0 = (T / R) * R;
+      if (r0 == T) {
+        slot = extra;
+        build_list(h, x, slot);
+      } else {
+        const int b = ((T - 1) / E) * E;
+        int rc = segment(b);
+        if (rc) return rc;
+        slot = (r0 - b) / R;
+      }
     } else {
       const int b = (n / E) * E;
-      if (b != seg) {
-        // recompute states b .. b + E - 1 (those below T) from checkpoint b / E
-        CK(cudaMemcpyAsync(h->seg_x, h->ckpt + (size_t)(b / E) * nd, sizeof(double) * nd,
-                           cudaMemcpyDeviceToDevice, h->stream));
-        build_list(h, h->seg_x, 0);
-        const int last = std::min(b + E - 1, T - 1);
-        for (int q = 1; q <= last - b; q++) {
-          const double* prev = h->seg_x + (size_t)(q - 1) * nd;
-          double* nx = h->seg_x + (size_t)q * nd;
-          step(h, prev, q - 1, h->xi + (size_t)(b + q - 1) * nd, nx, F_STEP);
-          build_list(h, nx, q);
-        }
-        seg = b;
-      }
+      int rc = segment(b);
+      if (rc) return rc;
       x = h->seg_x + (size_t)(n - b) * nd;
-      slot = n - b;
+      slot = (n - b) / R;
     }
     int flags = n >= T - h->K + 1 ? F_LOSS : 0;
     if (n < T) flags |= F_STEP;

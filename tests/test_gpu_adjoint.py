@@ -37,10 +37,13 @@ def _dense_laws(w):
     return laws
 
 
-def test_adjoint_matches_dense_autograd():
+@pytest.mark.parametrize("steps,E", [(40, 7), (43, 8)])
+def test_adjoint_matches_dense_autograd(steps, E):
+    """E = 7: one list per state; E = 8: each list serves 8 states (skin),
+    with a final state that does not start a list."""
     from pyrdsim_gb300 import workloads
     from pyrdsim_gb300.adjoint import trajectory_loss
-    w, adj, xi, x0, K = _setup()
+    w, adj, xi, x0, K = _setup(steps=steps, E=E)
     theta = torch.tensor(w["theta"], dtype=torch.float64, requires_grad=True)
     x0g = x0.clone().requires_grad_(True)
     loss = trajectory_loss(x0g, workloads.mixed_lj_yukawa_params(theta), xi, adj)
@@ -91,17 +94,63 @@ def test_adjoint_matches_finite_differences():
 
 
 def test_checkpoint_interval_does_not_change_results():
+    """Bit for bit across checkpoint intervals with the same list reuse
+    (E = 1, 7: one list per state; E = 32, 64: eight states per list);
+    within float64 rounding between the two."""
     from pyrdsim_gb300 import workloads
-    out = []
-    for E in (1, 7, 64):
-        w, adj, xi, x0, K = _setup(n=1024, steps=30, K=30, E=E)
+    out = {}
+    for E in (1, 7, 32, 64):
+        w, adj, xi, x0, K = _setup(n=1024, steps=70, K=70, E=E)
         loss, xT = adj.forward(x0, workloads.mixed_lj_yukawa_params(w["theta"]), xi)
         gx, gp = adj.backward()
-        out.append((loss, xT.cpu().numpy(), gx.cpu().numpy(), gp.numpy()))
-    for o in out[1:]:
-        assert o[0] == out[0][0]
-        for a, b in zip(o[1:], out[0][1:]):
-            np.testing.assert_array_equal(a, b)
+        out[E] = (loss, xT.cpu().numpy(), gx.cpu().numpy(), gp.numpy())
+    for a, b in ((1, 7), (32, 64)):
+        assert out[a][0] == out[b][0]
+        for u, v in zip(out[a][1:], out[b][1:]):
+            np.testing.assert_array_equal(u, v)
+    assert abs(out[1][0] - out[32][0]) <= 1e-12 * abs(out[1][0])
+    for u, v in zip(out[1][1:], out[32][1:]):
+        np.testing.assert_allclose(u, v, rtol=1e-9, atol=1e-9 * np.abs(v).max())
+
+
+def test_list_reuse_falls_back_when_a_particle_outruns_the_skin():
+    """Two particles placed 0.65 apart repel at about 19,000 per unit
+    mobility: their first step moves them farther than the skin allows, the
+    forward pass notices and repeats with one list per state, and the
+    results match a handle that never reuses lists."""
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.adjoint import Adjoint
+    w = workloads.mixed_lj_yukawa(n=256, seed=8)
+    x = np.array(w["x0"])
+    L = np.asarray(w["L"])
+    # the closest pair (a, b) brought to 0.65 along its axis; b stays more
+    # than 1.4 from everything else
+    d = x[:, None] - x[None]
+    d -= L * np.round(d / L)
+    r = np.sqrt((d ** 2).sum(-1))
+    np.fill_diagonal(r, np.inf)
+    a, b = np.unravel_index(np.argmin(r), r.shape)
+    u = -d[a, b] / r[a, b]  # unit vector from a to b
+    x[b] = x[a] + 0.65 * u
+    x0 = torch.tensor(np.mod(x, L), dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(3)
+    xi = torch.tensor(rng.standard_normal((16, 256, 2)), dtype=torch.float64, device="cuda")
+    p = workloads.mixed_lj_yukawa_params(w["theta"])
+    res = []
+    for E in (7, 8):
+        adj = Adjoint(2, w["L"], w["dt"], w["mobility"], w["types"],
+                      workloads.mixed_lj_yukawa_laws(w), loss_steps=8, checkpoint_every=E)
+        loss, _ = adj.forward(x0, p, xi)
+        assert adj.states_per_list == 1
+        gx, gp = adj.backward()
+        res.append((loss, gx.cpu().numpy(), gp.numpy()))
+    calm = Adjoint(2, w["L"], w["dt"], w["mobility"], w["types"],
+                   workloads.mixed_lj_yukawa_laws(w), loss_steps=8, checkpoint_every=8)
+    calm.forward(torch.tensor(w["x0"], dtype=torch.float64, device="cuda"), p, xi)
+    assert calm.states_per_list == 8
+    assert abs(res[0][0] - res[1][0]) <= 1e-12 * abs(res[0][0])
+    np.testing.assert_allclose(res[1][1], res[0][1], rtol=1e-9, atol=1e-9 * np.abs(res[0][1]).max())
+    np.testing.assert_allclose(res[1][2], res[0][2], rtol=1e-9)
 
 
 def test_backward_scales_and_guards_generations():
