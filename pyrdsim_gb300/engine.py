@@ -230,6 +230,29 @@ class Engine:
                                       counts.ctypes.data_as(C.POINTER(C.c_int64))))
         return counts
 
+    def time_series(self, n_steps, every, sys=0, rdf=None, noise=True):
+        """Step ``n_steps`` steps (Philox noise) and sample the observables of
+        system ``sys`` after every ``every`` steps: a dict of arrays (one
+        entry per sample: energies, virial, minimum distance, pair count,
+        type counts [samples, MAX_TYPES], and the step index).  With
+        ``rdf=dict(r_max=..., n_bins=..., type_a=..., type_b=...)`` also the
+        summed pair-distance histogram over the samples ("rdf_counts")."""
+        if every < 1 or n_steps < every:
+            raise ValueError("need 1 <= every <= n_steps")
+        rows, hist = [], None
+        for _ in range(n_steps // every):
+            self.step(every, noise=noise)
+            o = self.observables(sys)
+            o["step"] = self.step_index
+            rows.append(o)
+            if rdf is not None:
+                c = self.rdf_counts(sys=sys, **rdf)
+                hist = c if hist is None else hist + c
+        out = {k: np.array([r[k] for r in rows]) for k in rows[0]}
+        if hist is not None:
+            out["rdf_counts"] = hist
+        return out
+
     def rdf(self, r_max, n_bins=100, type_a=-1, type_b=-1, sys=0, other_molecules=False):
         """Radial distribution function g(r) at the bin centres: the pair
         histogram divided by the count an ideal gas of the same densities

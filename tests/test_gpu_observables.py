@@ -145,3 +145,16 @@ def test_observables_reject_bad_arguments():
         eng.rdf_counts(1.0, 0)
     with pytest.raises(EngineError):
         eng.rdf_counts(1.0, 100000)
+
+
+def test_time_series_samples_observables():
+    sd = _workload("active_wall_fluid_4096")
+    eng = _engine([sd])
+    ts = eng.time_series(200, 20, rdf=dict(r_max=3.0, n_bins=30))
+    assert ts["pair_energy"].shape == (10,)
+    np.testing.assert_array_equal(ts["step"], np.arange(20, 201, 20))
+    assert (ts["type_counts"].sum(axis=1) == sd.n_particles).all()
+    assert ts["rdf_counts"].shape == (30,) and ts["rdf_counts"].sum() > 0
+    # the last sample equals a direct call at the same state
+    last = eng.observables()
+    assert last["pair_energy"] == ts["pair_energy"][-1]
