@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-precision", action="store_true")
     return p.parse_args()
 
 
@@ -171,20 +172,155 @@ def cpu_baseline(workload, n_gpu_state=None):
     }
 
 
-def force_error(eng, sd):
-    """Drift of the GPU engine vs the float64 oracle on the same state."""
+def fp64_drift(sd, x, types, device):
+    """Plain PyTorch float64 drift of one system at positions x: the pair laws
+    (pyrdsim.pyx:1068-1130) over every pair of different molecules within
+    each law's cutoff (the (small, large) type pair as listed; minimum image
+    in periodic dimensions), the walls (pyrdsim.pyx:1132-1145; the 9-3 wall
+    cut at rc) and the bonds (pyrdsim.pyx:2037-2047).  Dense in chunks of
+    rows; angle terms are not covered."""
     import numpy as np
-    from oracle.oracle import Oracle
+    import torch
+    m = sd.model
+    D, N = m.N_dim, sd.n_particles
+    f64 = dict(dtype=torch.float64, device=device)
+    X = torch.tensor(np.asarray(x)[:, :D], **f64)
+    T = torch.tensor(np.asarray(types), dtype=torch.long, device=device)
+    mol = torch.tensor(sd.molecule_ids[:, 0], dtype=torch.long, device=device)
+    L = torch.tensor(np.asarray(m.L, dtype=float)[:D], **f64)
+    per = torch.tensor(np.asarray(m.periodic, dtype=float)[:D] > 0, device=device)
+    laws = [sd.inter[q] for q in range(sd.struct.n_interactions)]
+    pair_laws = [w for w in laws if 1 <= w.law <= 5 and w.type_a <= w.type_b]
+    walls = [w for w in laws if w.law in (6, 7)]
+
+    def law_f(w, r):
+        if w.law == 1:
+            s = (w.r0 / r) ** w.n
+            return -2.0 * w.n * w.u0 / r * s * (s - 1.0)
+        if w.law == 2:
+            return w.u0 * (1.0 - torch.tanh((r - w.r0) / w.a) ** 2) / (2.0 * w.a)
+        if w.law == 3:
+            return -w.u0 * (1.0 + w.r0 / r) * torch.exp(-r / w.r0) / (r * w.r0)
+        if w.law == 4:
+            return w.u0 * r
+        return torch.where(r < w.r0 - w.dr, torch.zeros_like(r), torch.full_like(r, w.u0 / w.dr))
+
+    a = torch.zeros_like(X)
+    ch = max(1, (1 << 27) // N)
+    for i0 in range(0, N, ch):
+        i1 = min(N, i0 + ch)
+        d = X[None, :, :] - X[i0:i1, None, :]
+        d = torch.where(per, d - L * torch.round(d / L), d)
+        r = torch.sqrt((d * d).sum(-1))
+        other = (mol[i0:i1, None] != mol[None, :]) & (r > 0)
+        lo = torch.minimum(T[i0:i1, None], T[None, :])
+        hi = torch.maximum(T[i0:i1, None], T[None, :])
+        rs = torch.where(other, r, torch.ones_like(r))
+        fr = torch.zeros_like(r)
+        for w in pair_laws:
+            rc = w.r0 if w.law == 5 else w.rc
+            mask = other & (lo == w.type_a) & (hi == w.type_b) & (r <= rc)
+            fr = fr + torch.where(mask, law_f(w, rs) / rs, torch.zeros_like(r))
+        a[i0:i1] += (fr[..., None] * d).sum(1)
+        del d, r, other, lo, hi, rs, fr
+    for w in walls:
+        sel = T == w.type_a
+        y = X[:, w.type_b]
+        if w.law == 6:
+            f = w.u0 * (1.0 - torch.tanh((y - w.r0) / w.a) ** 2) / (2.0 * w.a)
+        else:
+            sr = w.r0 / y
+            f = torch.where(y <= w.rc, w.u0 / y * (-1.2 * sr ** 9 + 3.0 * sr ** 3), torch.zeros_like(y))
+        a[:, w.type_b] -= torch.where(sel, f, torch.zeros_like(f))
+    # bonds of every molecule
+    i1s, i2s, ks, r0s = [], [], [], []
+    tmpl = {sd.tmpl[q].molecule_id: sd.tmpl[q] for q in range(sd.struct.n_templates)}
+    for first in sd.first_index:
+        tp = tmpl.get(int(sd.molecule_ids[first, 2]))
+        if tp is None:
+            continue
+        for e in range(tp.first_term, tp.first_term + tp.n_terms):
+            tm = sd.terms[e]
+            if tm.kind == 1:
+                i1s.append(first + tm.i)
+                i2s.append(first + tm.j)
+                ks.append(tm.k0)
+                r0s.append(tm.p0)
+    if i1s:
+        i1 = torch.tensor(i1s, device=device)
+        i2 = torch.tensor(i2s, device=device)
+        v = X[i2] - X[i1]
+        v = torch.where(per, v - L * torch.round(v / L), v)
+        dist = torch.sqrt((v * v).sum(-1))
+        f = torch.tensor(ks, **f64) * (dist - torch.tensor(r0s, **f64))
+        g = (f / dist)[:, None] * v
+        a.index_add_(0, i1, g)
+        a.index_add_(0, i2, -g)
+    return a.cpu().numpy()
+
+
+def force_error(eng, sd, device):
+    """Drift of the GPU engine (float32 pair and bonded forces) against the
+    float64 PyTorch drift at the same state, right after a rebuild."""
+    import numpy as np
     x, t = eng.state()
     eng.set_state(x, t)
-    o = Oracle(sd, history_quirk=False)
-    o.set_state(x, t)
-    a, r = eng.drift(), o.drift()
+    x, t = eng.state()
+    a, r = eng.drift(), fp64_drift(sd, x, t, device)
     norm = float(np.linalg.norm(a - r) / np.linalg.norm(r))
     mag = np.linalg.norm(r, axis=1)
     floor = float(np.sqrt(np.mean(mag ** 2)))
     per = float((np.linalg.norm(a - r, axis=1) / np.maximum(mag, floor)).max())
     return {"norm": norm, "per_particle_rms_floor": per}
+
+
+def precision_report(local):
+    """Force error against float64 for every configuration's shape, and the
+    trajectory error of the reaction-free LJ fluid after 100 steps with the
+    same injected normals (float64 PyTorch integration)."""
+    import numpy as np
+    import torch
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    dev = f"cuda:{local}"
+    out = {}
+    cases = {
+        "cfg1_lj_fluid_n1024": workloads.lj_fluid(n=1024),
+        "cfg3_patchy_colloids_n65536": workloads.patchy_colloids(n_molecules=16384),
+        "cfg4_ensemble_8_systems": None,
+    }
+    for name, sd in cases.items():
+        if sd is None:
+            errs = []
+            for e in workloads.ensemble(n_systems=8, seed=4):
+                errs.append(force_error(Engine([e], device=local), e, dev))
+            out[name] = {"norm": max(q["norm"] for q in errs),
+                         "per_particle_rms_floor": max(q["per_particle_rms_floor"] for q in errs)}
+        else:
+            out[name] = force_error(Engine([sd], device=local), sd, dev)
+    # trajectory: 100 steps of the LJ fluid, noise injected into both
+    sd = workloads.lj_fluid(n=1024)
+    eng = Engine([sd], device=local)
+    x0, t0 = eng.state()
+    rng = np.random.default_rng(11)
+    xi = rng.standard_normal((100, sd.n_particles, 2))
+    eng.step(100, xi=xi, u1=np.ones((100, sd.n_particles)), u2=np.ones((100, sd.n_particles)))
+    xg, _ = eng.state()
+    m = sd.model
+    L = np.asarray(m.L, dtype=float)[:2]
+    D_t = float(m.tau_by_tauD[0])
+    x = x0.copy()
+    for k in range(100):
+        a = fp64_drift(sd, x, t0, dev)
+        x = x + m.dt * D_t * a
+        x = x + np.sqrt(2.0 * m.dt * D_t) * xi[k]
+        x = np.mod(x, L)
+    d = xg - x
+    d -= L * np.round(d / L)
+    out["cfg1_lj_fluid_n1024_positions_after_100_steps"] = {
+        "max_abs": float(np.abs(d).max()),
+        "max_rel": float((np.abs(d) / np.maximum(np.abs(x), 1.0)).max())}
+    return out
 
 
 def ensemble_comparison(local, steps=100, n_systems=512):
@@ -360,7 +496,7 @@ def run_ours(args, rank, ws, local):
         except Exception as exc:
             out["cpu_baseline"] = {"unavailable": str(exc)[:200]}
         try:
-            out["force_err_vs_fp64"] = force_error(eng, sd)
+            out["force_err_vs_fp64"] = force_error(eng, sd, f"cuda:{local}")
         except Exception as exc:
             out["force_err_vs_fp64"] = {"unavailable": str(exc)[:200]}
     if rank == 0 and ws == 1 and not args.no_ensemble:
@@ -369,6 +505,11 @@ def run_ours(args, rank, ws, local):
             out["ensemble"] = ensemble_comparison(local)
         except Exception as exc:
             out["ensemble"] = {"unavailable": str(exc)[:200]}
+    if rank == 0 and ws == 1 and not args.no_precision:
+        try:
+            out["precision_vs_fp64"] = precision_report(local)
+        except Exception as exc:
+            out["precision_vs_fp64"] = {"unavailable": str(exc)[:200]}
     if rank == 0 and ws == 1 and not args.no_adjoint:
         try:
             out["adjoint"] = adjoint_timing(local)
