@@ -180,3 +180,33 @@ def test_adjoint_rejects_bad_systems():
         bad = law("lj", (0, 0), 1.0, 1.12, 2.5)
         bad.law = 2
         Adjoint(2, [10.0, 10.0], 1e-4, [1.0], np.zeros(8, np.int32), [bad], loss_steps=1)
+
+
+def test_adjoint_3d_matches_dense_autograd():
+    """A 3D periodic LJ + Yukawa mixture (512 particles, density 0.4)."""
+    from pyrdsim_gb300.adjoint import Adjoint, law, trajectory_loss
+    rng = np.random.default_rng(12)
+    n, rho = 512, 0.4
+    L = (n / rho) ** (1.0 / 3.0)
+    g = int(round(n ** (1.0 / 3.0)))
+    grid = (np.stack(np.meshgrid(*[np.arange(g)] * 3, indexing="ij"), -1).reshape(-1, 3) + 0.5)
+    x = (grid * (L / g) + rng.uniform(-0.05, 0.05, (n, 3)) * (L / g)) % L
+    types = (rng.random(n) < 0.5).astype(np.int32)
+    r0 = 2.0 ** (1.0 / 6.0)
+    laws = [law("lj", (0, 0), 1.0, r0, 2.5), law("lj", (0, 1), 1.0, r0, 2.5),
+            law("lj", (1, 1), 1.0, r0, 2.5), law("yukawa", (1, 1), 5.0, 0.5, 3.0)]
+    adj = Adjoint(3, [L, L, L], 1e-4, [1.0, 1.0], types, laws, loss_steps=6, checkpoint_every=4)
+    xi = torch.tensor(rng.standard_normal((12, n, 3)), dtype=torch.float64, device="cuda")
+    params = torch.tensor([[w.u0, w.r0] for w in laws], dtype=torch.float64, requires_grad=True)
+    x0 = torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=True)
+    loss = trajectory_loss(x0, params, xi, adj)
+    loss.backward()
+    pd = params.detach().clone().cuda().requires_grad_(True)
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=True)
+    dl = [(LAW_LJ, 6, 0, 0, 2.5), (LAW_LJ, 6, 0, 1, 2.5), (LAW_LJ, 6, 1, 1, 2.5),
+          (LAW_YUKAWA, 0, 1, 1, 3.0)]
+    ref = dense_loss(xd, pd, xi, types, dl, [L, L, L], 1e-4, [1.0, 1.0], 6)
+    ref.backward()
+    assert abs(loss.item() - ref.item()) <= 1e-12 * abs(ref.item())
+    assert float((x0.grad - xd.grad).norm() / xd.grad.norm()) <= 1e-9
+    np.testing.assert_allclose(params.grad.numpy(), pd.grad.cpu().numpy(), rtol=1e-9)
