@@ -88,3 +88,29 @@ def test_relaxed_initial_conditions_on_the_gpu():
         assert np.isfinite(out[:, 4:]).all()
         assert s._engine.observables()["min_distance"] >= m.rs / 10
         assert os.path.exists(m.initial_conditions_filename)
+
+
+@pytest.mark.parametrize("n_dim", [2, 3])
+def test_random_rotations_are_proper_rotations(n_dim):
+    from pyrdsim_gb300 import initial_conditions as ic
+    R = ic.random_rotations(500, n_dim, np.random.default_rng(1))
+    eye = np.broadcast_to(np.eye(n_dim), R.shape)
+    np.testing.assert_allclose(R @ np.swapaxes(R, 1, 2), eye, atol=1e-12)
+    np.testing.assert_allclose(np.linalg.det(R), 1.0, atol=1e-12)
+    # products of 1..99 turns of up to 10 degrees cover all angles in 2D
+    if n_dim == 2:
+        ang = np.arctan2(R[:, 0, 1], R[:, 0, 0])
+        assert np.histogram(ang, bins=8, range=(-np.pi, np.pi))[0].min() > 20
+
+
+def test_rdf_normalisation_of_an_ideal_gas():
+    from pyrdsim_gb300.engine import rdf_normalise
+    rng = np.random.default_rng(2)
+    L, n = 40.0, 4000
+    x = rng.random((n, 2)) * L
+    d = x[:, None, :] - x[None, :, :]
+    d -= L * np.round(d / L)
+    r = np.sqrt((d ** 2).sum(-1))[np.triu_indices(n, 1)]
+    counts, _ = np.histogram(r, bins=40, range=(0.0, 8.0))
+    rc, g, _ = rdf_normalise(counts, 8.0, 2, L * L, n * (n - 1) / 2)
+    assert abs(g.mean() - 1.0) < 0.02 and np.abs(g[5:] - 1.0).max() < 0.1
