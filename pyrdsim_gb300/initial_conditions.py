@@ -10,7 +10,7 @@ the one whose first atom lies farthest from the first atoms already placed
 whole system with a full ``simulate()`` run after every insertion.
 
 Here the placement rule is the same, with the nearest-first-atom distances
-from a k-d tree of the placed first atoms (rebuilt every few hundred
+from a k-d tree of the placed first atoms (rebuilt every 64
 insertions, the newest ones compared directly), and the relaxation runs once
 for the finished system on the GPU engine (``simulate`` with its noise),
 followed by the reference's check that no two listed partners of different
@@ -78,6 +78,16 @@ def random_rotations(n, n_dim, rng):
     planes = [(i, j) for i in range(n_dim) for j in range(i + 1, n_dim)]
     n_rot = rng.choice(np.arange(1, 100), size=n)
     angle = rng.random(n) * 10.0 * np.pi / 180.0
+    if n_dim == 2:
+        # one plane: the product of n_rot turns by angle is one turn by
+        # n_rot * angle
+        t = n_rot * angle
+        c, s = np.cos(t), np.sin(t)
+        out[:, 0, 0] = c
+        out[:, 1, 1] = c
+        out[:, 0, 1] = s
+        out[:, 1, 0] = -s
+        return out
     c, s = np.cos(angle), np.sin(angle)
     # exp(angle * G) for the generator G with G[i, j] = 1, G[j, i] = -1
     factors = np.tile(np.eye(n_dim), (len(planes), n, 1, 1))
@@ -112,7 +122,7 @@ class _Nearest:
     """Nearest distance from query points to a growing set of points: a
     k-d tree of the older points plus a direct comparison with the newest."""
 
-    def __init__(self, n_dim, rebuild_every=256):
+    def __init__(self, n_dim, rebuild_every=64):
         self.pts = np.zeros((0, n_dim))
         self.tree = None
         self.n_tree = 0
