@@ -41,7 +41,11 @@ import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_PYX = "/root/reference/pyrdsim/pyrdsim.pyx"
+# The reference checkout: $PYRDSIM_REFERENCE, else the read-only mount of
+# the build container.  Absent (as on the GPU machines): nothing to cythonize.
+REF_ROOT = os.environ.get("PYRDSIM_REFERENCE", "/root/reference")
+REF_PYX = os.path.join(REF_ROOT, "pyrdsim", "pyrdsim.pyx")
+REF_EXAMPLES = os.path.join(REF_ROOT, "examples")
 
 _EXPOSE = [
     ("np.ndarray x # current positions", "readonly np.ndarray x # current positions"),

@@ -7,7 +7,9 @@ in parallel and linked into one plain shared library with a C ABI
 """
 from __future__ import annotations
 
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 
@@ -38,13 +40,34 @@ def sources():
     return out
 
 
+STAMP = LIB + ".stamp"
+
+
+def _stamp(nvcc, flags):
+    """Machine, compiler, flags and source contents of a build: the library is
+    reused only by a build with the same stamp (a copy made on another
+    machine, e.g. x86-64 for an Arm host, is recompiled)."""
+    h = hashlib.sha256()
+    h.update(platform.machine().encode())
+    h.update(subprocess.run([nvcc, "--version"], capture_output=True, text=True).stdout.encode())
+    h.update(" ".join(flags + UNITS).encode())
+    for s in sources():
+        with open(s, "rb") as f:
+            h.update(s.encode() + f.read())
+    return h.hexdigest()
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
-    if not force and os.path.exists(LIB):
-        if os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in sources()):
-            return LIB
     nvcc = _nvcc()
     flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", *ARCH]
+    stamp = _stamp(nvcc, flags)
+    if not force and os.path.exists(LIB) and os.path.exists(STAMP):
+        with open(STAMP) as f:
+            if f.read().strip() == stamp:
+                print(f"librdsim: reusing {LIB} (stamp {stamp[:12]}, {platform.machine()})")
+                return LIB
+    print(f"librdsim: compiling for sm_103a on {platform.machine()} (stamp {stamp[:12]})")
     if verbose:
         flags.insert(0, "-Xptxas=-v")
     objs, procs = [], []
@@ -57,6 +80,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise subprocess.CalledProcessError(max(codes), "nvcc")
     subprocess.check_call([nvcc, "-shared", *ARCH, "-o", LIB + ".tmp", *objs])
     os.replace(LIB + ".tmp", LIB)
+    with open(STAMP, "w") as f:
+        f.write(stamp + "\n")
     return LIB
 
 

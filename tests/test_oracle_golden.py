@@ -5,9 +5,10 @@ reference's own outputs for small seeded decks, run on its own mt19937 stream.
 The oracle replays the same decks on the same stream (ORACLE_STREAM) with the
 reference's shallow-copy neighbour-list history (history_quirk=True).
 
-Bars: integer results (types, cell ids, neighbour pairs) exact; float64
-positions, drift and rates to 1e-9 relative -- the only difference left is the
-summation order of pair forces (the reference iterates Python sets).
+Bars: integer results (types, cell ids, neighbour pairs) and float64
+positions (final state and every trajectory frame) bit for bit; drift and
+rates to 1e-9 relative -- the reference sums pair forces in Python-set order,
+which moves the drift by an ulp without changing any position.
 """
 import numpy as np
 import pytest
@@ -47,13 +48,13 @@ def test_run_matches_reference_stream(name):
         traj.append(o.state())
     x, t = o.state()
     np.testing.assert_array_equal(t, fx["final_types"])
-    assert _close(x, fx["final_x"])
+    np.testing.assert_array_equal(x, fx["final_x"])
     assert _close(o.drift(), fx["final_a"])
     np.testing.assert_array_equal(o.cell_ids().reshape(-1), fx["final_cell_ids"])
     assert pair_set(o.pairs()) == pair_set(fx["final_pairs"])
     assert _close(o.reaction_rates(recompute=False), fx["final_total_rates"], floor=1.0)
     for k, (xk, tk) in enumerate(traj):
-        assert _close(xk, fx["trajectory"][k])
+        np.testing.assert_array_equal(xk, fx["trajectory"][k])
         np.testing.assert_array_equal(tk, fx["trajectory_types"][k])
 
 

@@ -6,7 +6,7 @@ import pytest
 
 from helpers import CASE_NAMES, deck_dict, in_deck, load_fixture
 
-REF_EXAMPLES = "/root/reference/examples"
+from oracle.build_ref import REF_EXAMPLES  # $PYRDSIM_REFERENCE/examples
 
 
 def test_parses_golden_decks_like_the_oracle_inputs():
