@@ -210,15 +210,16 @@ int rdsim_get_pairs(rdsim_handle* h, int32_t sys, int32_t* pairs,
                     int64_t cap, int64_t* n_pairs);
 
 /* No counterpart in the reference.  The same sorted pair list as
- * rdsim_get_pairs, for callers that cannot allocate device memory (code that
- * runs during another thread's CUDA graph capture, loops that must avoid the
- * device-wide synchronisation of cudaFree, processes whose device memory is
- * all in a preallocated pool).  It calls no cudaMalloc/cudaFree: its scratch
- * is a static device array of RDSIM_STATIC_PAIRS_MAX pairs (8 MiB, held by
- * every GPU that loads the library until exit).  More pairs than that return
- * RDSIM_ERR_CAPACITY.  The first call on a device looks the array up and
- * should come before any stream capture; concurrent calls race on the
- * shared array. */
+ * rdsim_get_pairs, for callers that cannot allocate device memory: processes
+ * whose device memory is already committed (a preallocated pool, another
+ * framework's cache), where cudaMalloc fails, and loops that must not pay the
+ * device-wide synchronisation of cudaFree.  It calls no cudaMalloc/cudaFree:
+ * its scratch is a static device array of RDSIM_STATIC_PAIRS_MAX pairs
+ * (8 MiB, held by every GPU that loads the library until exit).  More pairs
+ * than that return RDSIM_ERR_CAPACITY.  The first call on a device (and the
+ * first after its context is recreated, e.g. by cudaDeviceReset) looks the
+ * array up and loads the pair kernels of every dimension.  Concurrent calls
+ * race on the shared array. */
 #define RDSIM_STATIC_PAIRS_MAX (1LL << 20)
 int rdsim_get_pairs_static(rdsim_handle* h, int32_t sys, int32_t* pairs,
                            int64_t cap, int64_t* n_pairs);

@@ -4,6 +4,7 @@
 // concatenated; re-sorted at every neighbour-list rebuild):
 //   xh[buf][k][i]  u32  high word of the 64-bit fixed-point coordinate k
 //   xl[buf][k][i]  u32  low word
+//   xp[buf][k][i]  u32  pair word: bits ps_k .. ps_k + 31 of the coordinate
 //   meta[buf][i]   u32  type | type_at_rebuild << 8 | local atom << 16 |
 //                       template << 24 (0xff = no bonded terms)
 //   mol[buf][i]    i32  molecule number (initial-condition column 0)
@@ -11,9 +12,15 @@
 // Fixed point per dimension k of a system with box length L:
 //   periodic   : X in [0, 2^64) represents X * L / 2^64 (wraps exactly)
 //   reflecting : X in [0, S], S = 2^63 - 2^34, represents X * L / S
-// The pair kernels use only the high words: (int32)(hj - hi) * unit_hi is
-// the minimum-image displacement in float32 for periodic dimensions and the
-// plain displacement for reflecting ones.
+// The pair kernels read only the pair words: (int32)(pj - pi) is the
+// displacement in units of q_k = (length per fixed unit) * 2^ps_k, the
+// minimum image in periodic dimensions (the wrap of X at 2^64 carries over
+// to the 32-bit difference) and the plain displacement in reflecting ones.
+// ps_k is the smallest shift whose range (2^31 q_k) holds twice the largest
+// per-dimension separation of listed pairs, so q_k is about 1e-9 to 1e-8
+// length units whatever the box length.  The squared distance is formed from
+// the exact integer squares d_k^2, each rounded once to float32.  The
+// cell-list rebuild uses the high words (bits 32..63).
 #pragma once
 
 #include <cstdint>
@@ -44,7 +51,7 @@ struct WallLaw {
   float c0, c1, c2, c3;
   float rc_lo, rc_hi;             // 9-3 wall: guard band around rc (length units)
   double r0, rc;
-  long long hr0;                  // high-word fixed value of r0 (tanh wall)
+  long long hr0;                  // fixed-point value of r0 (tanh wall)
 };
 
 // One reaction (pyrdsim.pyx:2070-2223).
@@ -60,6 +67,7 @@ struct TermDev {                  // bonded term; angles in radians
   int kind, i, j, k;
   float p0, k0, thr;
   float pi;                       // angle: +1 if its theta0 == pi, else -1
+  unsigned long long r0q_lo, r0q_hi;  // bond: r0^2 in fixed units^2 (128 bits)
 };
 
 struct TmplDev {
@@ -86,6 +94,14 @@ struct SysDev {
   long long Si[3];                // reflecting: fixed value of L
   float unit_hi[3];               // length per high-word unit
   float inv_unit_hi[3];
+  float unitf[3];                 // length per fixed unit (float32)
+  int ps[3];                      // pair-word shift
+  float qf[3];                    // length per pair-word unit
+  float q2[3];                    // its square
+  // Bonds: with one fixed unit in every dimension, squared bond lengths are
+  // exact 128-bit integers in units of unit^2 (bonded_terms).
+  int bond128;                    // 1: every dimension has the same unit
+  float unit2f;                   // unit^2 as float32
   float delta;                    // allowed displacement since the last
                                   // rebuild (Euclidean, length units)
   unsigned long long hrange[3];   // high-word range used for cell mapping
@@ -137,6 +153,7 @@ struct Args {
   const int* cell_start;
   const uint32_t* xh[3];
   const uint32_t* xl[3];
+  const uint32_t* xp[3];          // pair words
   const uint32_t* meta;
   const int* mol;
   const int* pid;
@@ -144,6 +161,7 @@ struct Args {
   const uint32_t* xr[3];          // high words at the last rebuild
   uint32_t* xh_out[3];
   uint32_t* xl_out[3];
+  uint32_t* xp_out[3];
   uint32_t* meta_out;
   float* drift[3];
   double* rates_out;              // reaction-rate hook (sorted order)

@@ -34,11 +34,15 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+// A failing runtime call also sets the thread's last-error state; it is
+// cleared here so that a later launch check does not report it again.
 #define CK(call)                                                                  \
   do {                                                                            \
     cudaError_t e_ = (call);                                                      \
-    if (e_ != cudaSuccess)                                                        \
+    if (e_ != cudaSuccess) {                                                      \
+      cudaGetLastError();                                                         \
       return fail(RDSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                             \
   } while (0)
 
 constexpr double TWO32 = 4294967296.0;
@@ -59,7 +63,10 @@ template <class T>
 int dalloc(T** p, size_t n, int64_t* acc) {
   if (n == 0) n = 1;
   cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
-  if (e != cudaSuccess) return fail(RDSIM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the non-sticky allocation error
+    return fail(RDSIM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
   *acc += (int64_t)(n * sizeof(T));
   return 0;
 }
@@ -109,6 +116,7 @@ struct rdsim_handle {
   int *cell_of = nullptr, *rank_of = nullptr, *tmp = nullptr, *sid = nullptr, *slot_of = nullptr;
   uint32_t* xh[2][3] = {};
   uint32_t* xl[2][3] = {};
+  uint32_t* xp[2][3] = {};          // pair words (see device.cuh)
   uint32_t* xr[3] = {};
   uint32_t* meta[2] = {};
   int* mol[2] = {};
@@ -218,8 +226,10 @@ Args make_args(rdsim_handle* h) {
   for (int k = 0; k < 3; k++) {
     a.xh[k] = h->xh[h->cx][k];
     a.xl[k] = h->xl[h->cx][k];
+    a.xp[k] = h->xp[h->cx][k];
     a.xh_out[k] = h->xh[1 - h->cx][k];
     a.xl_out[k] = h->xl[1 - h->cx][k];
+    a.xp_out[k] = h->xp[1 - h->cx][k];
     a.xr[k] = h->xr[k];
     a.drift[k] = h->drift[k];
   }
@@ -456,6 +466,7 @@ int upload_state(rdsim_handle* h) {
   for (int k = 0; k < 3; k++) {
     a.xh[k] = h->xh[0][k];
     a.xl[k] = h->xl[0][k];
+    a.xp[k] = h->xp[0][k];
   }
   a.meta = h->meta[0];
   a.mol = h->mol[0];
@@ -559,7 +570,7 @@ void free_all(rdsim_handle* h) {
   F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
   F(h->chunks_d); F(h->nbr); F(h->ncnt); F(h->rx_list); F(h->rx_count);
   for (int b = 0; b < 2; b++) {
-    for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); }
+    for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); F(h->xp[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
   }
   for (int k = 0; k < 3; k++) { F(h->xr[k]); F(h->drift[k]); }
@@ -580,10 +591,10 @@ void free_all(rdsim_handle* h) {
 }
 
 // Half-width of the guard band around r^2 inside which the float64 distance
-// decides.  The kernels' float32 r^2 from high words errs by less than
-// 5e-7 r^2 (rounding of the unit, the conversion, the products and the sum)
-// plus 2 r sqrt(3) unit (truncation of both coordinates); the band is four
-// times wider.
+// decides.  The kernels' float32 r^2 from pair words errs by less than
+// 5e-7 r^2 (rounding of the squares, the unit and the sum) plus 2 r sqrt(3)
+// unit (truncation of both coordinates to the word's unit); the band is
+// four times wider.
 // The smallest float32 not below v (v >= 0).
 float float_up(double v) {
   float f = (float)v;
@@ -697,6 +708,29 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       }
       max_unit = std::max(max_unit, (double)sd.unit_hi[k]);
     }
+    // Pair words (device.cuh): listed pairs are at most (list radius + 2
+    // delta) <= 2 rs apart at any step of a rebuild period (rs bounds the
+    // list radius, rebuilt every freq steps, and the displacement check
+    // stops a call before a particle exceeds delta); the shift is the
+    // smallest whose range 2^31 q holds twice that.
+    double max_q = 0;
+    {
+      const double sep = 2.0 * std::max(S.rs, 1e-3) + 8.0 * max_unit;
+      for (int k = 0; k < D; k++) {
+        int ps = 0;
+        while (ps < 32 && std::ldexp(sd.unit_d[k], ps + 31) < 2.0 * sep) ps++;
+        sd.ps[k] = ps;
+        const double q = std::ldexp(sd.unit_d[k], ps);
+        sd.qf[k] = (float)q;
+        sd.q2[k] = (float)(q * q);
+        sd.unitf[k] = (float)sd.unit_d[k];
+        max_q = std::max(max_q, q);
+      }
+      sd.bond128 = 1;
+      for (int k = 1; k < D; k++)
+        if (sd.unit_d[k] != sd.unit_d[0]) sd.bond128 = 0;
+      sd.unit2f = (float)(sd.unit_d[0] * sd.unit_d[0]);
+    }
     // reference cell geometry for the cell-id hook (pyrdsim.pyx:1436-1444)
     if (S.rs > 0 && S.cell_length_ratio > 0) {
       for (int k = 0; k < D; k++) {
@@ -790,12 +824,12 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
           L.rin = it.r0 - it.dr;
           break;
       }
-      float g = guard2(rc, max_unit);
+      float g = guard2(rc, max_q);
       L.rc2_lo = (float)(rc * rc) - g;
       L.rc2_hi = (float)(rc * rc) + g;
       if (it.law == RDSIM_LAW_PIECEWISE_LINEAR) {
         double ri = std::max(0.0, L.rin);
-        float gi2 = guard2(ri, max_unit);
+        float gi2 = guard2(ri, max_q);
         L.in2_lo = (float)(ri * ri) - gi2;
         L.in2_hi = (float)(ri * ri) + gi2;
       }
@@ -856,7 +890,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         } else {
           return bail(fail(RDSIM_ERR_ARG, "unknown reaction kind"));
         }
-        float g = guard2(r.r0, max_unit);
+        float g = guard2(r.r0, max_q);
         x.r02_lo = (float)(r.r0 * r.r0) - g;
         x.r02_hi = (float)(r.r0 * r.r0) + g;
         Rrx2 = std::max(Rrx2, x.r02_hi);
@@ -979,6 +1013,17 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
           d.k0 = (float)tr.k0;
           d.thr = (float)(tr.p0 - 0.1);
           d.pi = std::fabs(tr.p0 - M_PI) <= 1e-5 + 1e-5 * M_PI ? 1.f : -1.f;  // np.isclose
+          if (tr.kind == RDSIM_TERM_BOND && sd.bond128) {
+            // r0^2 in units of unit^2 as a 128-bit integer: (r0 / unit)
+            // rounded to an integer, squared exactly (its rounding moves
+            // r0 by under one fixed unit)
+            const double v = std::min(std::fabs(tr.p0) / sd.unit_d[0], 1.8e19);
+            if (!(v < 9.2e18)) sd.bond128 = 0;  // a rest length beyond the box
+            const unsigned __int128 r = (unsigned __int128)(unsigned long long)std::llround(std::min(v, 9.2e18));
+            const unsigned __int128 r2 = v < 9.2e18 ? r * r : ~(unsigned __int128)0;
+            d.r0q_lo = (unsigned long long)r2;
+            d.r0q_hi = (unsigned long long)(r2 >> 64);
+          }
           int ti = (int)terms.size();
           terms.push_back(d);
           oterms.push_back(tr);
@@ -1119,6 +1164,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     for (int k = 0; k < D; k++) {
       if ((rc = dalloc(&h->xh[b][k], N, &B))) return bail(rc);
       if ((rc = dalloc(&h->xl[b][k], N, &B))) return bail(rc);
+      if ((rc = dalloc(&h->xp[b][k], N, &B))) return bail(rc);
     }
     if ((rc = dalloc(&h->meta[b], N, &B))) return bail(rc);
     if ((rc = dalloc(&h->mol[b], N, &B))) return bail(rc);
@@ -1349,8 +1395,12 @@ int rdsim_get_pairs(rdsim_handle* h, int32_t sys, int32_t* pairs, int64_t cap, i
   unsigned long long* cnt = nullptr;
   int* buf = nullptr;
   size_t bcap = (size_t)std::max<int64_t>(cap, 1);
-  CK(cudaMalloc(&cnt, sizeof(unsigned long long)));
+  if (cudaMalloc(&cnt, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(RDSIM_ERR_NOMEM, "pair counter");
+  }
   if (cudaMalloc(&buf, sizeof(int) * 2 * bcap) != cudaSuccess) {
+    cudaGetLastError();
     cudaFree(cnt);
     return fail(RDSIM_ERR_NOMEM, "pair buffer");
   }
@@ -1416,12 +1466,16 @@ int rdsim_get_observables(rdsim_handle* h, int32_t sys, rdsim_observables* out) 
     if (h->obs_part) cudaFree(h->obs_part);
     h->obs_part = nullptr;
     h->obs_cap = 0;
-    if (cudaMalloc(&h->obs_part, sizeof(double) * ((size_t)nb + 1) * OBS_NSUM) != cudaSuccess)
+    if (cudaMalloc(&h->obs_part, sizeof(double) * ((size_t)nb + 1) * OBS_NSUM) != cudaSuccess) {
+      cudaGetLastError();
       return fail(RDSIM_ERR_NOMEM, "observables scratch");
+    }
     h->obs_cap = nb;
   }
-  if (!h->obs_counts && cudaMalloc(&h->obs_counts, sizeof(unsigned long long) * (1 + MAXT)) != cudaSuccess)
+  if (!h->obs_counts && cudaMalloc(&h->obs_counts, sizeof(unsigned long long) * (1 + MAXT)) != cudaSuccess) {
+    cudaGetLastError();
     return fail(RDSIM_ERR_NOMEM, "observables scratch");
+  }
   ObsArgs o;
   std::memset(&o, 0, sizeof o);
   o.laws = h->olaws_d;
@@ -1482,8 +1536,10 @@ int rdsim_get_rdf(rdsim_handle* h, int32_t sys, int32_t type_a, int32_t type_b, 
     o.h[k] = (int)std::min<double>(sd.nc[k], std::floor(reach / cell) + 1.0);
   }
   CK(cudaSetDevice(h->device));
-  if (!h->rdf_counts && cudaMalloc(&h->rdf_counts, sizeof(unsigned long long) * RDF_MAX_BINS) != cudaSuccess)
+  if (!h->rdf_counts && cudaMalloc(&h->rdf_counts, sizeof(unsigned long long) * RDF_MAX_BINS) != cudaSuccess) {
+    cudaGetLastError();
     return fail(RDSIM_ERR_NOMEM, "histogram scratch");
+  }
   o.counts = h->rdf_counts;
   o.r_max = r_max;
   o.width = r_max / n_bins;
@@ -1617,20 +1673,23 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
 //
 // rdsim_get_pairs allocates its device scratch (a pair counter and a pair
 // buffer) with cudaMalloc and releases it with cudaFree on every call.  Some
-// callers cannot do that: code that runs while another thread captures a
-// CUDA graph on the device, loops that must not pay the device-wide
-// synchronisation of cudaFree, or processes whose device memory is fully
-// committed to a preallocated pool.  rdsim_get_pairs_static computes the same
-// sorted pair list into the caller's host buffer with its scratch in the
-// static device array below instead.
+// callers cannot do that: processes whose device memory is fully committed
+// (a preallocated pool, another framework's cache), where cudaMalloc fails,
+// and loops that must not pay the device-wide synchronisation of cudaFree.
+// rdsim_get_pairs_static computes the same sorted pair list into the
+// caller's host buffer with its scratch in the static device array below
+// instead.
 //
 // The array is RDSIM_STATIC_PAIRS_MAX pairs (8 MiB) plus a counter; every GPU
 // that loads the library holds it until the process exits.  Its device
-// address is looked up once per device (cudaGetSymbolAddress, with that device
-// current) by the first call on that device; make that first call before any
-// stream capture.  All calls share the array: the counter is cleared at the
-// start of every call, and calls that overlap on the GPU (from several
-// threads or handles at once) race on it.
+// address belongs to the CUDA context that loaded the module: it is looked up
+// (cudaGetSymbolAddress, with that device current) by the first call in each
+// context on a device and again after the context changes (a cudaDeviceReset
+// makes a new primary context, and with it a new array), under a lock.  The
+// same set-up also loads k_pairs for every dimension, so that under lazy
+// module loading no later call loads code.  All calls share the array: the
+// counter is cleared at the start of every call, and calls that overlap on
+// the GPU (from several threads or handles at once) race on it.
 namespace {
 
 constexpr long long kStaticPairsMax = RDSIM_STATIC_PAIRS_MAX;
@@ -1638,18 +1697,68 @@ constexpr long long kStaticPairsMax = RDSIM_STATIC_PAIRS_MAX;
 static __device__ __align__(256) unsigned long long g_pairs_scratch[1 + kStaticPairsMax];
 
 constexpr int kMaxDevices = 64;
-unsigned long long* g_pairs_scratch_ptr[kMaxDevices] = {};
+struct ScratchSlot {
+  unsigned long long ctx_id = 0;   // context the address belongs to
+  bool valid = false;
+  unsigned long long* ptr = nullptr;
+};
+ScratchSlot g_pairs_slot[kMaxDevices];
+std::mutex g_pairs_mutex;
 
+// Current context's unique id (cuCtxGetId, through the runtime's driver entry
+// points: the library does not link the driver directly).  False if the
+// driver offers no such call; the address is then looked up on every call.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_pairs_mutex
+    looked_up = true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+      get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    cudaGetLastError();
+  }
+  if (!get_current || !get_id) return false;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx) return false;
+  return get_id(ctx, id) == 0;
+}
+
+// Device address of g_pairs_scratch in the current context of `device` (the
+// caller has made it current).
 int static_scratch(int device, unsigned long long** out) {
   if (device < 0 || device >= kMaxDevices) return fail(RDSIM_ERR_ARG, "device ordinal out of range");
-  if (!g_pairs_scratch_ptr[device]) {
+  std::lock_guard<std::mutex> lock(g_pairs_mutex);
+  unsigned long long id = 0;
+  const bool have_id = current_context_id(&id);
+  ScratchSlot& slot = g_pairs_slot[device];
+  if (!have_id || !slot.valid || slot.ctx_id != id) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_pairs_scratch);
     if (e != cudaSuccess)
       return fail(RDSIM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_pairs_scratch_ptr[device] = static_cast<unsigned long long*>(p);
+    // load the pair kernels of every dimension now (lazy loading would
+    // otherwise load each on its first launch)
+    cudaFuncAttributes fa;
+    const cudaError_t e1 = cudaFuncGetAttributes(&fa, k_pairs<1>);
+    const cudaError_t e2 = cudaFuncGetAttributes(&fa, k_pairs<2>);
+    const cudaError_t e3 = cudaFuncGetAttributes(&fa, k_pairs<3>);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+      return fail(RDSIM_ERR_CUDA, "loading the pair kernels failed");
+    slot.ptr = static_cast<unsigned long long*>(p);
+    slot.ctx_id = id;
+    slot.valid = have_id;
   }
-  *out = g_pairs_scratch_ptr[device];
+  *out = slot.ptr;
   return 0;
 }
 

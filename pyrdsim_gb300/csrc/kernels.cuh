@@ -150,15 +150,70 @@ __device__ double exact_dist(const SysDev& s, const Args& a, int gi, int gj) {
   return __dsqrt_rn(d2);
 }
 
-// f / r of one pair law at squared distance r2 (float32); inv_r2 = 1 / r2.
+// Reciprocal of r2 > 0: the hardware approximation and one Newton step
+// (within about one ulp).
+__device__ inline float recip(float r2) {
+  float w;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(w) : "f"(r2));
+  return fmaf(w, fmaf(-r2, w, 1.0f), w);
+}
+
+// f / r of the Lennard-Jones n = 6 law, g(w) = c0 s (s - 1) w with w = 1/r^2
+// and s = (c1 w)^3.  The law amplifies the relative error of w about
+// sevenfold (g ~ w^7 near contact), so the rounding of w is removed to first
+// order: with eta = w r2 - 1 (exact by fma), g(w / (1 + eta)) =
+// g(w) - eta w g'(w) and w g'(w) = c0 s (7 s - 4) w.
+__device__ inline float lj6_over_r(float c0, float c1, float r2, float w) {
+  const float eta = fmaf(w, r2, -1.0f);
+  const float q = c1 * w;  // (r0/r)^2
+  const float s = q * q * q;
+  const float cs = c0 * s;
+  const float g = cs * (s - 1.0f) * w;
+  return fmaf(-eta, cs * fmaf(7.0f, s, -4.0f) * w, g);
+}
+
+// Squared distance of a pair from its pair-word differences d_k (exact
+// integers): each d_k^2 is exact in 64 bits and rounded once to float32.
+template <int D>
+__device__ inline float pair_r2(const SysDev& s, const int* d) {
+  float r2 = 0.f;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    const long long dk = d[k];
+    r2 = fmaf(__ull2float_rn((unsigned long long)(dk * dk)), s.q2[k], r2);
+  }
+  return r2;
+}
+
+// A 128-bit unsigned integer rounded to the nearest float32: the top 64
+// significant bits, with the bits below them folded into a sticky bit (which
+// lies far below float32's rounding position), converted once.
+__device__ inline float u128_to_float(unsigned __int128 v) {
+  const unsigned long long hi = (unsigned long long)(v >> 64);
+  if (hi == 0ull) return __ull2float_rn((unsigned long long)v);
+  const int sh = 64 - __clzll((long long)hi);
+  const unsigned long long top = (unsigned long long)(v >> sh);
+  const unsigned long long sticky = ((unsigned long long)v << (64 - sh)) != 0ull ? 1ull : 0ull;
+  return ldexpf(__ull2float_rn(top | sticky), sh);
+}
+
+// Displacement x_j - x_i along dimension k from the full fixed-point words
+// (minimum image in periodic dimensions), rounded once to float32 before the
+// unit is applied: bonded terms, whose partners may lie anywhere in the box.
+__device__ inline float disp_full(const SysDev& s, const Args& a, int k, int gi, int gj) {
+  const unsigned long long Xi = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
+  const unsigned long long Xj = ((unsigned long long)a.xh[k][gj] << 32) | a.xl[k][gj];
+  return __ll2float_rn((long long)(Xj - Xi)) * s.unitf[k];
+}
+
+// f / r of one pair law at squared distance r2 (float32); inv_r2 = recip(r2).
 __device__ inline float eval_pair(const PairLaw& L, float r2, float inv_r2) {
   switch (L.law) {
     case RDSIM_LAW_LJ: {  // f = -2 n u0 / r * s (s - 1), s = (r0/r)^n
+      if (L.n == 6) return lj6_over_r(L.c0, L.c1, r2, inv_r2);
       const float q = L.c1 * inv_r2;  // (r0/r)^2
       float s;
-      if (L.n == 6) {
-        s = q * q * q;
-      } else if ((L.n & 1) == 0) {
+      if ((L.n & 1) == 0) {
         s = 1.0f;
         for (int e = 0; e < (L.n >> 1); e++) s *= q;
       } else {
@@ -193,7 +248,7 @@ template <int D>
 __device__ inline float pair_force(const SysDev& s, const PairLaw* laws, const Args& a, int gi,
                                    int gj, unsigned int pp, float r2) {
   const int nl = pp & 31, l0 = (pp >> 5) & 0x3ff;
-  const float inv_r2 = __fdividef(1.0f, r2);
+  const float inv_r2 = recip(r2);
   float fr = 0.f;
   double dexact = -1.0;
   for (int l = l0; l < l0 + nl; l++) {
@@ -350,6 +405,7 @@ __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid
     }
     a.xh_out[k][gi] = (uint32_t)(X >> 32);
     a.xl_out[k][gi] = (uint32_t)X;
+    a.xp_out[k][gi] = (uint32_t)(X >> s.ps[k]);
   }
 }
 
@@ -372,14 +428,39 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
     const int role = code & 3;
     if (tr.kind == RDSIM_TERM_BOND) {
       const int other = a.slot_of[mbase + (role == 0 ? tr.j : tr.i)];
-      float d2 = 0.f;
+      // f = k (d - r0) / d (pyrdsim.pyx:2037-2047).  A stiff bond near rest
+      // cancels in d - r0: where every dimension has the same fixed unit,
+      // d^2 - r0^2 is formed exactly in 128-bit integers (units unit^2) and
+      // d - r0 = (d^2 - r0^2) / (d + r0) keeps float32 precision relative
+      // to itself.  Otherwise the full-word float32 displacement is used.
+      float f;
+      if (s.bond128) {
+        unsigned __int128 S2 = 0;
 #pragma unroll
-      for (int k = 0; k < D; k++) {
-        xo[k] = (float)(int)(a.xh[k][other] - a.xh[k][gi]) * s.unit_hi[k];
-        d2 += xo[k] * xo[k];
+        for (int k = 0; k < D; k++) {
+          const unsigned long long Xi = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
+          const unsigned long long Xj = ((unsigned long long)a.xh[k][other] << 32) | a.xl[k][other];
+          const long long dd = (long long)(Xj - Xi);
+          const unsigned long long m = dd < 0 ? 0ull - (unsigned long long)dd : (unsigned long long)dd;
+          S2 += (unsigned __int128)m * m;
+          xo[k] = __ll2float_rn(dd) * s.unitf[k];
+        }
+        const unsigned __int128 R0 = ((unsigned __int128)tr.r0q_hi << 64) | tr.r0q_lo;
+        const bool longer = S2 >= R0;
+        const float ex = u128_to_float(longer ? S2 - R0 : R0 - S2) * s.unit2f;
+        const float d = sqrtf(u128_to_float(S2) * s.unit2f);
+        const float dmr = (longer ? ex : -ex) / (d + tr.p0);
+        f = tr.k0 * dmr / d;
+      } else {
+        float d2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+          xo[k] = disp_full(s, a, k, gi, other);
+          d2 = fmaf(xo[k], xo[k], d2);
+        }
+        const float d = sqrtf(d2);
+        f = tr.k0 * (d - tr.p0) / d;
       }
-      const float d = sqrtf(d2);
-      const float f = tr.k0 * (d - tr.p0) / d;
 #pragma unroll
       for (int k = 0; k < D; k++) acc[k] += f * xo[k];
     } else {
@@ -388,10 +469,10 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
       float v1[3], v2[3], n1 = 0.f, n2 = 0.f;
 #pragma unroll
       for (int k = 0; k < D; k++) {
-        v1[k] = (float)(int)(a.xh[k][s1] - a.xh[k][s2]) * s.unit_hi[k];
-        v2[k] = (float)(int)(a.xh[k][s3] - a.xh[k][s2]) * s.unit_hi[k];
-        n1 += v1[k] * v1[k];
-        n2 += v2[k] * v2[k];
+        v1[k] = disp_full(s, a, k, s2, s1);
+        v2[k] = disp_full(s, a, k, s2, s3);
+        n1 = fmaf(v1[k], v1[k], n1);
+        n2 = fmaf(v2[k], v2[k], n2);
       }
       const float d21 = sqrtf(n1), d23 = sqrtf(n2);
       float c = 0.f, sn;
@@ -456,9 +537,12 @@ __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const A
       const float e = expf(-2.0f * fabsf(z));
       f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
     } else {
-      // reflecting coordinates are signed (an initial position may be < 0)
-      const float y = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) *
-                      s.unit_hi[W.dim];
+      // the full coordinate; reflecting ones are signed (an initial
+      // position may lie below 0)
+      const unsigned long long X = ((unsigned long long)h << 32) | a.xl[W.dim][gi];
+      const float y = (((s.periodic >> W.dim) & 1) ? __ull2float_rn(X)
+                                                    : __ll2float_rn((long long)X)) *
+                      s.unitf[W.dim];
       if (y > W.rc_hi) continue;
       if (y >= W.rc_lo) {
         const double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
@@ -842,6 +926,7 @@ __global__ void k_order(Args a, OrderOut o, const int* tmp, const int* cell_of,
     const uint32_t h = a.xh[d][old];
     a.xh_out[d][fin] = h;
     a.xl_out[d][fin] = a.xl[d][old];
+    a.xp_out[d][fin] = a.xp[d][old];
     o.xr[d][fin] = h;
   }
   const uint32_t m = a.meta[old];
@@ -873,6 +958,7 @@ __global__ void k_to_double(const SysDev* sysv, const int* sid, Args a, double* 
 struct StateOut {
   uint32_t* xh[3];
   uint32_t* xl[3];
+  uint32_t* xp[3];
   uint32_t* meta;
   int* mol;
   int* pid;
@@ -903,6 +989,7 @@ __global__ void k_from_double(const SysDev* sysv, const int* sid, const double* 
     }
     a.xh[k][gi] = (uint32_t)(X >> 32);
     a.xl[k][gi] = (uint32_t)X;
+    a.xp[k][gi] = (uint32_t)(X >> s.ps[k]);
   }
   const int t = types[gi];
   if (t < 0 || t >= s.ntypes) {

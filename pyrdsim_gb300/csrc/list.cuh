@@ -269,7 +269,7 @@ __device__ inline int row_scan(const SysDev& s, const Args& a, int i, int lane, 
   return cnt;
 }
 
-// A list entry with the neighbour's current high words and meta word.
+// A list entry with the neighbour's current pair words and meta word.
 struct Nb {
   uint32_t x[3];
   uint32_t m;
@@ -282,9 +282,18 @@ __device__ inline Nb gather(const Args& a, int v) {
   const int j = v & 0x7fffffff;
   n.v = v;
 #pragma unroll
-  for (int k = 0; k < 3; k++) n.x[k] = k < D ? a.xh[k][j] : 0u;
+  for (int k = 0; k < 3; k++) n.x[k] = k < D ? a.xp[k][j] : 0u;
   n.m = a.meta[j];
   return n;
+}
+
+// Pair-word differences of an entry (exact) and its squared distance.
+template <int D>
+__device__ inline float pair_geom(const SysDev& s, const uint32_t* xj, const uint32_t* xi,
+                                  int* d) {
+#pragma unroll
+  for (int k = 0; k < D; k++) d[k] = (int)(xj[k] - xi[k]);
+  return pair_r2<D>(s, d);
 }
 
 // Visit the list entries of particle i on this lane (entries lane, lane +
@@ -517,7 +526,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   const int cnt = a.ncnt[i];
   uint32_t xo[3] = {0u, 0u, 0u};
 #pragma unroll
-  for (int k = 0; k < D; k++) xo[k] = a.xh[k][i];
+  for (int k = 0; k < D; k++) xo[k] = a.xp[k][i];
   const uint32_t mi = a.meta[i];
   prefetch_rows<TPP>(a, ch, cnt, active);
   __syncthreads();
@@ -527,29 +536,22 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     const int ti = mi & 0xff;
     for_entries<D, TPP>(s, a, i, lane, cnt, [&](const Nb& nb) {
       if (nb.v < 0) return;  // same molecule: reactions only
-      float dx[3], r2 = 0.f;
-#pragma unroll
-      for (int k = 0; k < D; k++) {
-        dx[k] = (float)(int)(nb.x[k] - xo[k]) * s.unit_hi[k];
-        r2 += dx[k] * dx[k];
-      }
+      int d[3];
+      const float r2 = pair_geom<D>(s, nb.x, xo, d);
       const int tj = nb.m & 0xff;
       if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
       const unsigned int pp = s.ppair[ti * MAXT + tj];
       const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
       float fr;
       if ((pp & 0x8000u) && r2 < L0.rc2_lo) {
-        // a single Lennard-Jones n = 6 law, clear of its cutoff: the
-        // arithmetic of eval_pair inline
-        const float inv_r2 = __fdividef(1.0f, r2);
-        const float q = L0.c1 * inv_r2;
-        const float s6 = q * q * q;
-        fr = L0.c0 * s6 * (s6 - 1.0f) * inv_r2;
+        // a single Lennard-Jones n = 6 law, clear of its cutoff: eval_pair's
+        // arithmetic inline
+        fr = lj6_over_r(L0.c0, L0.c1, r2, recip(r2));
       } else {
         fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
       }
 #pragma unroll
-      for (int k = 0; k < D; k++) acc[k] += fr * dx[k];
+      for (int k = 0; k < D; k++) acc[k] = fmaf(fr, (float)d[k] * s.qf[k], acc[k]);
     });
   }
 #pragma unroll
@@ -625,7 +627,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   const uint32_t mi = a.meta[i];
   uint32_t xo[3] = {0u, 0u, 0u};
 #pragma unroll
-  for (int k = 0; k < D; k++) xo[k] = a.xh[k][i];
+  for (int k = 0; k < D; k++) xo[k] = a.xp[k][i];
   prefetch_rows<TPP>(a, ch, cnt, active);
   __syncthreads();
   const SysDev& s = sh.sys;
@@ -634,12 +636,8 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   if (active && ((s.rx_nb_mask >> ti) & 1)) {
     const float Rrx2 = s.Rrx2;
     for_entries<D, TPP>(s, a, i, lane, cnt, [&](const Nb& nb) {
-      float r2 = 0.f;
-#pragma unroll
-      for (int k = 0; k < D; k++) {
-        const float d = (float)(int)(nb.x[k] - xo[k]) * s.unit_hi[k];
-        r2 += d * d;
-      }
+      int d[3];
+      const float r2 = pair_geom<D>(s, nb.x, xo, d);
       if (!(r2 < Rrx2)) return;
       const unsigned int rm = s.rxmatch[ti * MAXT + (nb.m & 0xff)];
       double dexact = -1.0;
@@ -732,17 +730,13 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
     if ((s.rx_nb_mask >> tm) & 1) {
       uint32_t xm[3] = {0u, 0u, 0u};
 #pragma unroll
-      for (int k = 0; k < D; k++) xm[k] = a.xh[k][m];
+      for (int k = 0; k < D; k++) xm[k] = a.xp[k][m];
       const float Rrx2 = s.Rrx2;
       auto count = [&](int v, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t mj) {
         const int j = v & 0x7fffffff;
         const uint32_t xj[3] = {x0, x1, x2};
-        float r2 = 0.f;
-#pragma unroll
-        for (int k = 0; k < D; k++) {
-          const float d = (float)(int)(xj[k] - xm[k]) * s.unit_hi[k];
-          r2 += d * d;
-        }
+        int d[3];
+        const float r2 = pair_geom<D>(s, xj, xm, d);
         if (!(r2 < Rrx2)) return;
         const unsigned int rmask = s.rxmatch[tm * MAXT + (mj & 0xff)];
         double dexact = -1.0;

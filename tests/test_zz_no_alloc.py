@@ -1,9 +1,9 @@
 """rdsim_get_pairs_static: the neighbour-pair entry point that allocates nothing.
 
-Callers that cannot allocate device memory (code running while another thread
-captures a CUDA graph, loops that must not pay cudaFree's device-wide
-synchronisation, processes whose device memory sits in a preallocated pool)
-use rdsim_get_pairs_static instead of rdsim_get_pairs.  It keeps its scratch
+Callers that cannot allocate device memory (processes whose device memory is
+already committed, e.g. to a preallocated pool, where cudaMalloc fails; loops
+that must not pay cudaFree's device-wide synchronisation) use
+rdsim_get_pairs_static instead of rdsim_get_pairs.  It keeps its scratch
 in a static device array, so its result must equal rdsim_get_pairs' result --
 also on a second call in a row, which reuses the array left by the first.
 
@@ -69,4 +69,44 @@ def test_static_pairs_capacity_errors():
                                         1, C.byref(n))
     assert rc == 20 and n.value > 1
     assert eng.lib.rdsim_get_pairs_static(eng.h, 5, None, 0, C.byref(n)) == 1
+    eng.close()
+
+
+def test_static_pairs_with_device_memory_full():
+    """The motivating caller: a process whose device memory is already
+    committed (here: one tensor holding all but 2-4 MiB of the free
+    memory).  The allocating entry point then fails with RDSIM_ERR_NOMEM,
+    while the static one still returns its pairs: it allocated nothing."""
+    import torch
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    sd = workloads.active_wall_fluid(n=40000, seed=9)
+    eng = Engine([sd])
+    lib, h = eng.lib, eng.h
+    ref = _pairs(lib, h, "rdsim_get_pairs")
+    need = 8 * len(ref)                     # bytes rdsim_get_pairs allocates
+    assert need > (4 << 20), need
+    _pairs(lib, h, "rdsim_get_pairs_static")  # set-up call
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info()
+    block = 2 << 20
+    # leaves between 2 and 4 MiB free: less than rdsim_get_pairs needs
+    hog = torch.empty(max(0, (free - (2 << 20)) // block * block), dtype=torch.uint8,
+                      device="cuda")
+    try:
+        left, _ = torch.cuda.mem_get_info()
+        assert left < need, (left, need)
+        got = _pairs(lib, h, "rdsim_get_pairs_static")
+        n = C.c_int64()
+        buf = np.empty((len(ref), 2), dtype=np.int32)
+        rc = lib.rdsim_get_pairs(h, 0, buf.ctypes.data_as(C.POINTER(C.c_int32)), len(ref),
+                                 C.byref(n))
+        assert rc == 3, rc  # RDSIM_ERR_NOMEM: the allocating call cannot run
+        again = _pairs(lib, h, "rdsim_get_pairs_static")
+    finally:
+        del hog
+        torch.cuda.empty_cache()
+    np.testing.assert_array_equal(got, ref)
+    np.testing.assert_array_equal(again, ref)
     eng.close()
