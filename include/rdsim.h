@@ -141,7 +141,10 @@ typedef struct {
   double skin;                    /* cell skin in length units; <= 0: auto    */
   int32_t threads_per_particle;   /* lanes sharing one particle's list: 1, 2,
                                      4 or 8; other values: 2                  */
-  int32_t unused0;                /* 0                                        */
+  int32_t force_precision;        /* 0: float32 pair and bonded forces from
+                                     the pair words (the default); 1: float64
+                                     forces, drift and increments with the
+                                     reference's formulas (the plain method) */
   int32_t use_graphs;             /* >= 0: replay whole rebuild periods as CUDA
                                      graphs (Philox noise); < 0: plain launches */
   int32_t list_width;             /* Verlet-list entries stored per particle;
@@ -302,7 +305,7 @@ typedef struct {
   double skin, cell_size_min, interaction_range;
   int64_t device_bytes;
   int32_t reaction_prefilter;     /* 1: on for this handle                    */
-  int32_t pad;
+  int32_t force_precision;        /* as in rdsim_options                      */
 } rdsim_info;
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 

@@ -1,6 +1,7 @@
 """Builds the CUDA engine ``pyrdsim_gb300/_lib/librdsim.so`` for sm_103a.
 
-Two translation units (``csrc/engine.cu``: the step engine and observables;
+Three translation units (``csrc/engine.cu``: the step engine and
+observables; ``csrc/force64.cu``: the float64 drift kernels;
 ``csrc/adjoint.cu``: the differentiable reaction-free steps) compiled by nvcc
 in parallel and linked into one plain shared library with a C ABI
 (``include/rdsim.h``, ``include/rdsim_adjoint.h``); no PyTorch headers.
@@ -29,7 +30,7 @@ def _nvcc():
     raise RuntimeError("nvcc not found")
 
 
-UNITS = ["engine.cu", "adjoint.cu"]
+UNITS = ["engine.cu", "force64.cu", "adjoint.cu"]
 
 
 def sources():

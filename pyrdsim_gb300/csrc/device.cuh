@@ -90,6 +90,7 @@ struct SysDev {
   int rx_nb_mask;                 // ... of a neighbour-dependent reaction
   double L[3];
   double unit_d[3];               // length per fixed unit
+  double inv_unit_d[3];           // fixed units per length
   double S[3];                    // reflecting: fixed value of L (as double)
   long long Si[3];                // reflecting: fixed value of L
   float unit_hi[3];               // length per high-word unit
@@ -164,6 +165,14 @@ struct Args {
   uint32_t* xp_out[3];
   uint32_t* meta_out;
   float* drift[3];
+  // float64 force mode (force64.cuh): drift, the laws, walls and bonded
+  // terms with their float64 deck parameters (same order as laws / walls /
+  // terms), and per system [2][MAXT]: dt D and sqrt(2 dt D) per type
+  double* drift_d[3];
+  const rdsim_interaction* olaws;
+  const rdsim_interaction* owalls;
+  const rdsim_term* oterms;
+  const double* typed;
   double* rates_out;              // reaction-rate hook (sorted order)
   ErrDev* err;
   const double* xi;               // injected normals for the EM step

@@ -20,6 +20,8 @@
 #include "../../include/rdsim.h"
 #include "device.cuh"
 #include "kernels.cuh"
+#include "force64.h"
+#include "launch.cuh"
 #include "list.cuh"
 #include "observe.cuh"
 
@@ -122,6 +124,10 @@ struct rdsim_handle {
   int* mol[2] = {};
   int* pid[2] = {};
   float* drift[3] = {};
+  // float64 force mode (force64.cuh)
+  bool f64 = false;
+  double* drift_d[3] = {};
+  double* typed_d = nullptr;           // [nsys][2][MAXT]: dt D, sqrt(2 dt D)
   double* rates = nullptr;
   double* xbuf = nullptr;  // float64 positions in caller order (hooks)
   int* tbuf = nullptr;
@@ -232,7 +238,12 @@ Args make_args(rdsim_handle* h) {
     a.xp_out[k] = h->xp[1 - h->cx][k];
     a.xr[k] = h->xr[k];
     a.drift[k] = h->drift[k];
+    a.drift_d[k] = h->drift_d[k];
   }
+  a.olaws = h->olaws_d;
+  a.owalls = h->owalls_d;
+  a.oterms = h->oterms_d;
+  a.typed = h->typed_d;
   a.meta = h->meta[h->cm];
   a.meta_out = h->meta[1 - h->cm];
   a.mol = h->mol[h->co];
@@ -254,25 +265,6 @@ Args make_args(rdsim_handle* h) {
   a.single = h->nsys == 1 ? 1 : 0;
   if (!h->chunks_h.empty()) a.chunk1 = h->chunks_h[0];
   return a;
-}
-
-// Kernel launch with programmatic stream serialization: the kernel may be
-// scheduled while the previous kernel of the stream still runs (its launch
-// and table staging overlap that kernel's tail); every kernel waits
-// (griddepcontrol.wait) before it reads what earlier work writes.
-template <class... P, class... A>
-void launch(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k, static_cast<P>(args)...);
 }
 
 template <int D, int TPP>
@@ -370,7 +362,8 @@ int force(rdsim_handle* h, long long step, int flags, const double* xi_next, boo
   a.xi = xi_next;
   {
     ProfScope ps(h, P_FORCE, 1);
-    launch_step_kernel(h, false, a);
+    if (h->f64) CK(launch_force64(h->D, h->ltpp, (unsigned)h->chunks_h.size(), h->stream, a));
+    else launch_step_kernel(h, false, a);
   }
   CK(cudaGetLastError());
   if (flags & F_EM) h->cx = 1 - h->cx;
@@ -410,7 +403,8 @@ int em(rdsim_handle* h, long long step, int flags, const double* xi) {
   a.xi = xi;
   unsigned g = nblk(h->N);
   ProfScope ps(h, P_EM, 1);
-  if (h->D == 2) launch(k_em<2>, g, 256, h->stream, a, h->sid);
+  if (h->f64) CK(launch_em64(h->D, g, h->stream, a, h->sid));
+  else if (h->D == 2) launch(k_em<2>, g, 256, h->stream, a, h->sid);
   else if (h->D == 3) launch(k_em<3>, g, 256, h->stream, a, h->sid);
   else launch(k_em<1>, g, 256, h->stream, a, h->sid);
   CK(cudaGetLastError());
@@ -573,7 +567,8 @@ void free_all(rdsim_handle* h) {
     for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); F(h->xp[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
   }
-  for (int k = 0; k < 3; k++) { F(h->xr[k]); F(h->drift[k]); }
+  for (int k = 0; k < 3; k++) { F(h->xr[k]); F(h->drift[k]); F(h->drift_d[k]); }
+  F(h->typed_d);
   F(h->rates); F(h->xbuf); F(h->tbuf); F(h->err); F(h->cl_d);
   F(h->meta_static_d); F(h->mol_static_d); F(h->flag_d);
   F(h->inj_xi); F(h->inj_u1); F(h->inj_u2); F(h->traj_x); F(h->traj_t);
@@ -621,6 +616,11 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   auto* h = new rdsim_handle();
   h->device = opt.device;
   h->D = systems[0].n_dim;
+  if (opt.force_precision != 0 && opt.force_precision != 1) {
+    delete h;
+    return fail(RDSIM_ERR_ARG, "force_precision must be 0 (float32) or 1 (float64)");
+  }
+  h->f64 = opt.force_precision == 1;
   h->nsys = n_systems;
   int rc = 0;
   auto bail = [&](int code) {
@@ -641,6 +641,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   std::vector<TermDev> terms;
   std::vector<rdsim_interaction> olaws, owalls;  // float64 copies, same order
   std::vector<rdsim_term> oterms;
+  std::vector<double> typed;  // per system: dt D and sqrt(2 dt D) per type
   std::vector<int> atomterm;
   std::vector<double> x_all;
   std::vector<int> t_all;
@@ -694,6 +695,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         sd.periodic |= 1 << k;
         hsys.periodic_mask |= 1 << k;
         sd.unit_d[k] = S.L[k] / TWO64;
+        sd.inv_unit_d[k] = TWO64 / S.L[k];
         sd.unit_hi[k] = (float)(S.L[k] / TWO32);
         sd.inv_unit_hi[k] = (float)(TWO32 / S.L[k]);
         sd.hrange[k] = 1ULL << 32;
@@ -702,6 +704,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         hsys.Si[k] = S_REFLECT;
         sd.S[k] = (double)S_REFLECT;
         sd.unit_d[k] = S.L[k] / (double)S_REFLECT;
+        sd.inv_unit_d[k] = (double)S_REFLECT / S.L[k];
         sd.unit_hi[k] = (float)(S.L[k] * TWO32 / (double)S_REFLECT);
         sd.inv_unit_hi[k] = (float)((double)S_REFLECT / (S.L[k] * TWO32));
         sd.hrange[k] = ((unsigned long long)S_REFLECT >> 32) + 1;
@@ -740,6 +743,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       }
     }
     // per-type prefactors (pyrdsim.pyx:488-496) and partners (1157-1263)
+    typed.resize(typed.size() + 2 * MAXT, 0.0);
+    double* td = typed.data() + typed.size() - 2 * MAXT;
     for (int t = 0; t < S.n_types; t++) {
       double tau = S.tau_by_tauD[t];
       if (tau < 0) {
@@ -748,6 +753,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       } else {
         sd.fp[t] = (float)(S.dt * tau);
         sd.npf[t] = (float)std::sqrt(2.0 * S.dt * tau);
+        td[t] = S.dt * tau;
+        td[MAXT + t] = std::sqrt(2.0 * S.dt * tau);
       }
     }
     auto add_partner = [&](int a, int b) -> bool {
@@ -1173,7 +1180,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   for (int k = 0; k < D; k++) {
     if ((rc = dalloc(&h->xr[k], N, &B))) return bail(rc);
     if ((rc = dalloc(&h->drift[k], N, &B))) return bail(rc);
+    if (h->f64 && (rc = dalloc(&h->drift_d[k], N, &B))) return bail(rc);
   }
+  if ((rc = dalloc(&h->typed_d, typed.size(), &B))) return bail(rc);
   if ((rc = dalloc(&h->rates, N, &B))) return bail(rc);
   if ((rc = dalloc(&h->xbuf, (size_t)N * D, &B))) return bail(rc);
   if ((rc = dalloc(&h->tbuf, N, &B))) return bail(rc);
@@ -1215,11 +1224,15 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   if ((rc = up(h->oterms_d, oterms.data(), sizeof(rdsim_term) * oterms.size()))) return bail(rc);
   if ((rc = up(h->sid, sid_h.data(), sizeof(int) * sid_h.size()))) return bail(rc);
   if ((rc = up(h->cl_d, cl.data(), sizeof(double) * cl.size()))) return bail(rc);
+  if ((rc = up(h->typed_d, typed.data(), sizeof(double) * typed.size()))) return bail(rc);
   if (cudaMemsetAsync(h->err, 0, sizeof(ErrDev), h->stream) != cudaSuccess)
     return bail(fail(RDSIM_ERR_CUDA, "memset"));
-  for (int k = 0; k < D; k++)
+  for (int k = 0; k < D; k++) {
     if (cudaMemsetAsync(h->drift[k], 0, sizeof(float) * N, h->stream) != cudaSuccess)
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
+    if (h->f64 && cudaMemsetAsync(h->drift_d[k], 0, sizeof(double) * N, h->stream) != cudaSuccess)
+      return bail(fail(RDSIM_ERR_CUDA, "memset"));
+  }
   if ((rc = up(h->meta_static_d, h->meta_static.data(), sizeof(uint32_t) * (size_t)N))) return bail(rc);
   if ((rc = up(h->mol_static_d, h->mol_h.data(), sizeof(int) * (size_t)N))) return bail(rc);
   if ((rc = up(h->xbuf, x_all.data(), sizeof(double) * x_all.size()))) return bail(rc);
@@ -1362,15 +1375,22 @@ int rdsim_get_drift(rdsim_handle* h, double* a) {
   CK(cudaSetDevice(h->device));
   const int N = h->N, D = h->D;
   std::vector<float> d[3];
+  std::vector<double> dd[3];
   std::vector<int> pid(N);
   for (int k = 0; k < D; k++) {
-    d[k].resize(N);
-    CK(cudaMemcpyAsync(d[k].data(), h->drift[k], 4 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+    if (h->f64) {
+      dd[k].resize(N);
+      CK(cudaMemcpyAsync(dd[k].data(), h->drift_d[k], 8 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+    } else {
+      d[k].resize(N);
+      CK(cudaMemcpyAsync(d[k].data(), h->drift[k], 4 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+    }
   }
   CK(cudaMemcpyAsync(pid.data(), h->pid[h->co], 4 * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   for (int i = 0; i < N; i++)
-    for (int k = 0; k < D; k++) a[(size_t)pid[i] * D + k] = (double)d[k][i];
+    for (int k = 0; k < D; k++)
+      a[(size_t)pid[i] * D + k] = h->f64 ? dd[k][i] : (double)d[k][i];
   return 0;
 }
 
@@ -1663,6 +1683,7 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
   info->interaction_range = h->range;
   info->device_bytes = h->device_bytes;
   info->reaction_prefilter = (h->rx_pre && h->has_rx) ? 1 : 0;
+  info->force_precision = h->f64 ? 1 : 0;
   return 0;
 }
 

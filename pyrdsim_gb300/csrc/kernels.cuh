@@ -41,7 +41,7 @@ __device__ inline long long eff_em_step(const Args& a) {
   return a.step_base ? *a.step_base + a.em_step : a.em_step;
 }
 
-__global__ void k_set_counter(long long* c, long long v, int add) {
+static __global__ void k_set_counter(long long* c, long long v, int add) {
   pdl_trigger();
   pdl_wait();
   if (add) *c += v;
@@ -362,6 +362,36 @@ __device__ inline void gaussians(const U4& w, float* xi) {
   }
 }
 
+// Advances coordinate k of particle gi by d fixed units and applies the
+// boundary condition (pyrdsim.pyx:2253-2292): an exact wrap in periodic
+// dimensions, a reflection at 0 and L in 128-bit arithmetic in reflecting
+// ones (2 S overflows int64).  Writes the high, low and pair words.
+__device__ inline void advance(const SysDev& s, const Args& a, int gi, int pid, int k,
+                               long long d, long long em_step) {
+  unsigned long long X = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
+  if ((s.periodic >> k) & 1) {
+    X += (unsigned long long)d;
+  } else {
+    // reflect (pyrdsim.pyx:2275-2280)
+    __int128 Xs = (__int128)(long long)X + d;
+    const __int128 Si = s.Si[k];
+    if (Xs > Si) Xs = 2 * Si - Xs;
+    if (Xs < 0) Xs = -Xs;
+    if (Xs < 0 || Xs > Si) {
+      record_error(a.err, RDSIM_ERR_OUT_OF_BOUNDS, pid, k,
+                   __dmul_rn(__ll2double_rn((long long)(Xs > Si ? Si : 0)), s.unit_d[k]) +
+                       __dmul_rn(__ll2double_rn((long long)(Xs > Si ? Xs - Si : Xs)),
+                                 s.unit_d[k]),
+                   em_step);
+      Xs = Xs < 0 ? 0 : Si;
+    }
+    X = (unsigned long long)(long long)Xs;
+  }
+  a.xh_out[k][gi] = (uint32_t)(X >> 32);
+  a.xl_out[k][gi] = (uint32_t)X;
+  a.xp_out[k][gi] = (uint32_t)(X >> s.ps[k]);
+}
+
 // Euler-Maruyama update + boundary conditions of one particle in fixed point
 // (pyrdsim.pyx:2240-2292): x += dt D a + sqrt(2 dt D) xi, then reflect or wrap.
 template <int D>
@@ -383,29 +413,8 @@ __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid
     bool bad = false;
     float dl = fp * acc[k] + np * xi[k];
     long long d = delta_fixed(dl, s.inv_unit_hi[k], &bad);
-    unsigned long long X = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
     if (bad) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)dl, em_step);
-    if ((s.periodic >> k) & 1) {
-      X += (unsigned long long)d;
-    } else {
-      // reflect (pyrdsim.pyx:2275-2280) in 128-bit arithmetic: 2*S overflows int64
-      __int128 Xs = (__int128)(long long)X + d;
-      const __int128 Si = s.Si[k];
-      if (Xs > Si) Xs = 2 * Si - Xs;
-      if (Xs < 0) Xs = -Xs;
-      if (Xs < 0 || Xs > Si) {
-        record_error(a.err, RDSIM_ERR_OUT_OF_BOUNDS, pid, k,
-                     __dmul_rn(__ll2double_rn((long long)(Xs > Si ? Si : 0)), s.unit_d[k]) +
-                         __dmul_rn(__ll2double_rn((long long)(Xs > Si ? Xs - Si : Xs)),
-                                   s.unit_d[k]),
-                     em_step);
-        Xs = Xs < 0 ? 0 : Si;
-      }
-      X = (unsigned long long)(long long)Xs;
-    }
-    a.xh_out[k][gi] = (uint32_t)(X >> 32);
-    a.xl_out[k][gi] = (uint32_t)X;
-    a.xp_out[k][gi] = (uint32_t)(X >> s.ps[k]);
+    advance(s, a, gi, pid, k, d, em_step);
   }
 }
 
@@ -774,7 +783,7 @@ constexpr int SCAN_TILE = 256 * SCAN_ITEMS;
 constexpr int SCAN1_T = 1024;
 constexpr int SCAN1_I = 32;
 
-__global__ void __launch_bounds__(SCAN1_T) k_scan_one(const int* count, int n, int* start) {
+static __global__ void __launch_bounds__(SCAN1_T) k_scan_one(const int* count, int n, int* start) {
   pdl_trigger();
   pdl_wait();
   __shared__ int ws[SCAN1_T / 32];
@@ -820,7 +829,7 @@ __global__ void __launch_bounds__(SCAN1_T) k_scan_one(const int* count, int n, i
   }
 }
 
-__global__ void k_scan_partial(const int* count, int n, int* bsum) {
+static __global__ void k_scan_partial(const int* count, int n, int* bsum) {
   pdl_trigger();
   pdl_wait();
   __shared__ int ws[8];
@@ -840,7 +849,7 @@ __global__ void k_scan_partial(const int* count, int n, int* bsum) {
   }
 }
 
-__global__ void k_scan_final(const int* count, int n, const int* bsum, int* start) {
+static __global__ void k_scan_final(const int* count, int n, const int* bsum, int* start) {
   pdl_trigger();
   pdl_wait();
   __shared__ int ws[8];
@@ -885,7 +894,7 @@ __global__ void k_scan_final(const int* count, int n, const int* bsum, int* star
 }
 
 // Also zeroes the cell counts (consumed by the scans) for the next rebuild.
-__global__ void k_scatter(const int* cell_of, const int* rank_of, const int* start, int n,
+static __global__ void k_scatter(const int* cell_of, const int* rank_of, const int* start, int n,
                           int* tmp, int* count, int ncells) {
   pdl_trigger();
   pdl_wait();

@@ -107,10 +107,15 @@ class Engine:
     """
 
     def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, use_graphs=True,
-                 list_width=0, reaction_prefilter=None, autotune=False):
+                 list_width=0, reaction_prefilter=None, autotune=False, precision="float32"):
         """``autotune=True`` picks ``skin`` and ``threads_per_particle`` by
         timing short runs of this batch (:mod:`pyrdsim_gb300.autotune`,
-        cached per workload)."""
+        cached per workload).  ``precision="float64"`` evaluates pair and
+        bonded forces, the drift and the position increments in float64 with
+        the reference's formulas (the plain method); the default float32
+        path keeps float64 only where decisions must match the reference."""
+        if precision not in ("float32", "float64"):
+            raise ValueError("precision must be 'float32' or 'float64'")
         self.lib = load_library()
         self.systems = list(systems)
         if autotune:
@@ -118,7 +123,8 @@ class Engine:
             best = _tune(self.systems, device=device)
             skin = best["skin"]
             threads_per_particle = best["threads_per_particle"] or 0
-        self.options = {"skin": skin, "threads_per_particle": threads_per_particle}
+        self.options = {"skin": skin, "threads_per_particle": threads_per_particle,
+                        "precision": precision}
         self.D = self.systems[0].model.N_dim
         self.offsets = np.cumsum([0] + [s.n_particles for s in self.systems])
         self.N = int(self.offsets[-1])
@@ -129,6 +135,7 @@ class Engine:
         opt.threads_per_particle = threads_per_particle
         opt.use_graphs = 0 if use_graphs else -1
         opt.list_width = list_width
+        opt.force_precision = 1 if precision == "float64" else 0
         # None: automatic; True: whenever the rates allow; False: off
         opt.reaction_prefilter = 0 if reaction_prefilter is None else (1 if reaction_prefilter else -1)
         h = C.c_void_p()

@@ -19,7 +19,9 @@ Differences, all deliberate:
   keeps pairs listed at earlier rebuilds);
 * GPU options are extra dictionary keys starting with ``gpu_``:
   ``gpu_device``, ``gpu_skin``, ``gpu_threads_per_particle``,
-  ``gpu_list_width``, and ``gpu_angle_theta0_per_term`` (True: each angle
+  ``gpu_list_width``, ``gpu_precision`` ("float32": float32 pair and
+  bonded forces, the default; "float64": the reference's float64 forces,
+  drift and increments), and ``gpu_angle_theta0_per_term`` (True: each angle
   uses its own theta0 == pi test, not the late-bound flag of the last angle
   defined, pyrdsim.pyx:1401).
 """
@@ -183,7 +185,8 @@ class system:  # noqa: N801  (the reference's class name)
         eng = Engine([sd], device=int(self._gpu.get("device", 0)),
                      skin=float(self._gpu.get("skin", 0.0)),
                      threads_per_particle=int(self._gpu.get("threads_per_particle", 0)),
-                     list_width=int(self._gpu.get("list_width", 0)))
+                     list_width=int(self._gpu.get("list_width", 0)),
+                     precision=str(self._gpu.get("precision", "float32")))
         self._engine = eng
         if verbose:
             print("Creating neighbor list and evaluating drift..done", end="\n")

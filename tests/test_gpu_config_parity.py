@@ -65,6 +65,29 @@ def test_lj_fluid_1024():
     _run(workloads.lj_fluid(n=1024), 100, 1)
 
 
+def test_lj_fluid_1024_float64_plain_method():
+    """The configuration's float64 plain method (precision="float64"):
+    drift within 1e-12, positions after 100 injected steps within 1e-11."""
+    from oracle.oracle import Oracle
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    sd = workloads.lj_fluid(n=1024)
+    eng = Engine([sd], precision="float64")
+    orc = Oracle(sd, history_quirk=False)
+    norm, per = drift_errors(eng.drift(), orc.drift())
+    assert norm <= 1e-12 and per <= 1e-12, (norm, per)
+    rng = np.random.default_rng(12)
+    xi = rng.standard_normal((100, sd.n_particles, 2))
+    u = np.ones((10, sd.n_particles))
+    for c in range(10):
+        eng.step(10, xi=xi[10 * c:10 * (c + 1)], u1=u, u2=u)
+        orc.step(10, xi=xi[10 * c:10 * (c + 1)], u1=u, u2=u)
+    xg, _ = eng.state()
+    xo, _ = orc.state()
+    d = min_image(xg - xo, sd)
+    assert (np.abs(d) <= 1e-11 * np.maximum(np.abs(xo), 1.0)).all(), np.abs(d).max()
+
+
 def test_active_wall_fluid_65536():
     from pyrdsim_gb300 import workloads
     changed = _run(workloads.active_wall_fluid(n=65536), 20, 2)
