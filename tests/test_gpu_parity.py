@@ -397,6 +397,8 @@ def test_float64_mode_graph_replay_and_batching():
             graph.step(n)
         np.testing.assert_array_equal(plain.state()[0], graph.state()[0])
         np.testing.assert_array_equal(plain.state()[1], graph.state()[1])
+    # 2D decks sharing neighbor_list_update_frequency = 10
+    sds = [_case(nm)[1] for nm in ["lj_periodic", "two_species_wall_rx", "patchy", "angle_pi"]]
     batch = _engine(sds, precision="float64")
     batch.step(25)
     xb, tb = batch.state()
