@@ -188,10 +188,12 @@ struct Args {
   int* nbr_out;
   int* ncnt_out;
   int W, npad;                    // list width and particle stride
-  int4* rx_list;                  // [2][npad]: particles whose reaction draw
-                                  // may succeed at a step of that parity, as
-                                  // {sorted index, meta, list entries, pid}
-  int* rx_count;                  // [2]
+  int4* rx_list;                  // [3][npad]: particles whose reaction draw
+                                  // may succeed at a step, in slot step % 3,
+                                  // as {sorted index, meta, list entries, pid}
+  int* rx_count;                  // [3]
+  uint32_t* rtype;                // per particle: meta word after this step's
+                                  // reaction (drift kernel with F_RX_MERGED)
   const int* sid;                 // system of each particle
   int single;                     // one system: chunks follow from blockIdx
   Chunk chunk1;                   // ... with these table offsets
@@ -209,8 +211,25 @@ enum : int {
   F_RX_NEXT = 64,                 // drift kernel: copy the types forward and
                                   // list the particles whose reaction draw of
                                   // the next step may succeed
-  F_RX_HERE = 128                 // list builder: the same for its own step
+  F_RX_HERE = 128,                // list builder: the same for its own step
+  F_RX_MERGED = 256,              // drift kernel: first resolves this step's
+                                  // listed reaction draws itself (no reaction
+                                  // kernel ran), then writes every type
+  F_RX_FLAG = 512                 // drift kernel: mark the particles it lists
+                                  // (RX_PENDING) for a merged next step
 };
+
+// Meta-word bit of a particle listed for the next step's merged reaction
+// draw: its type byte is pending until the next drift kernel resolves it
+// (types are below 16, so the bit never belongs to a type).
+constexpr uint32_t RX_PENDING = 0x80u;
+
+// Slot of the candidate list of a step: three slots, so that a drift kernel
+// can read the slot of its own step, append to the next one and clear the
+// one after (consumed two steps earlier) without racing.
+__host__ __device__ inline int rx_slot(long long step) {
+  return (int)(((step % 3) + 3) % 3);
+}
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
 struct U4 {

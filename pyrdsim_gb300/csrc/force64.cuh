@@ -375,14 +375,14 @@ __global__ void __launch_bounds__(LBLOCK) k_force_d(Args a) {
     const unsigned int bal = __ballot_sync(0xffffffffu, listed);
     if (bal) {
       const int lane32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
-      const int p = (int)(eff_em_step(a) & 1);
+      const int p = rx_slot(eff_em_step(a));
       int base = 0;
       if (lane32 == leader) base = atomicAdd(a.rx_count + p, __popc(bal));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (listed) a.rx_list[(size_t)p * a.npad + base + __popc(bal & ((1u << lane32) - 1u))] = rec;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[eff_step(a) & 1] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[rx_slot(eff_step(a) + 2)] = 0;
 }
 
 // Stand-alone float64 EM update of every particle (first step of a call).

@@ -632,16 +632,14 @@ __device__ inline double rx_total(const SysDev& s, const RxDev* rx, int ti, cons
 // two comparisons are first made in float32 against the bounds of the
 // uniforms with a relative margin of 4e-6 (the float32 sums err by less than
 // 1e-6), and only an undecided comparison is redone in float64.
+// react_decide returns the new type of a type-ti particle (caller index pid)
+// at the kernel's step; react_tail writes it (or, with F_RATES_ONLY, the
+// total propensity).
 template <int D>
-__device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& a, int gi,
-                                  int pid, uint32_t mi, const uint32_t* cw) {
-  const int ti = mi & 0xff;
+__device__ inline int react_decide(const SysDev& s, const RxDev* rx, const Args& a, int pid,
+                                   int ti, const uint32_t* cw) {
   int newt = ti;
   const bool any = (s.rx_any_mask >> ti) & 1;
-  if (a.flags & F_RATES_ONLY) {
-    a.rates_out[pid] = any ? rx_total(s, rx, ti, cw) : 0.0;
-    return;
-  }
   if (any) {  // pyrdsim.pyx:2211-2222
     const long long step = eff_step(a);
     const bool inject = (a.flags & F_INJECT) != 0;
@@ -721,7 +719,18 @@ __device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& 
       if (pick < s.nrx) newt = rx[pick].product;
     }
   }
-  a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)newt;
+  return newt;
+}
+
+template <int D>
+__device__ inline void react_tail(const SysDev& s, const RxDev* rx, const Args& a, int gi,
+                                  int pid, uint32_t mi, const uint32_t* cw) {
+  const int ti = mi & 0xff;
+  if (a.flags & F_RATES_ONLY) {
+    a.rates_out[pid] = ((s.rx_any_mask >> ti) & 1) ? rx_total(s, rx, ti, cw) : 0.0;
+    return;
+  }
+  a.meta_out[gi] = (mi & 0xffffff00u) | (uint32_t)react_decide<D>(s, rx, a, pid, ti, cw);
 }
 
 // ---------------------------------------------------------------------------

@@ -493,11 +493,132 @@ __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Arg
     const unsigned int bal = __ballot_sync(0xffffffffu, listed);
     if (bal) {
       const int l32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
-      const int p = (int)(eff_step(a) & 1);
+      const int p = rx_slot(eff_step(a));
       int base = 0;
       if (l32 == leader) base = atomicAdd(a.rx_count + p, __popc(bal));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (listed) a.rx_list[(size_t)p * a.npad + base + __popc(bal & ((1u << l32) - 1u))] = rec;
+    }
+  }
+}
+
+// One listed particle's reaction draw at the kernel's step, by a whole warp
+// (pyrdsim.pyx:2070-2223): the lanes count, for every neighbour-dependent
+// reaction, its listed partners of the right type within r0 (types before
+// this step's reactions, positions of this step), and lane 0 forms the
+// propensities and draws.  rec = {sorted index, meta, list entries, pid}.
+// Returns the new type on lane 0.
+template <int D, int TPP>
+__device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Args& a, int4 rec,
+                                     int lane) {
+  const int m = rec.x, cnt = rec.z, pid = rec.w;
+  const uint32_t mm = (uint32_t)rec.y & ~RX_PENDING;
+  const int tm = mm & 0xff;
+  uint32_t cw[4] = {0u, 0u, 0u, 0u};
+  if ((s.rx_nb_mask >> tm) & 1) {
+    uint32_t xm[3] = {0u, 0u, 0u};
+#pragma unroll
+    for (int k = 0; k < D; k++) xm[k] = a.xp[k][m];
+    const float Rrx2 = s.Rrx2;
+    auto count = [&](const Nb& nb) {
+      const int j = nb.v & 0x7fffffff;
+      int d[3];
+      const float r2 = pair_geom<D>(s, nb.x, xm, d);
+      if (!(r2 < Rrx2)) return;
+      const unsigned int rmask = s.rxmatch[tm * MAXT + (nb.m & 0x7f)];
+      double dexact = -1.0;
+      for (unsigned int b = rmask; b; b &= b - 1u) {
+        const int r = __ffs(b) - 1;
+        const RxDev& R = rx[r];
+        bool inside;
+        if (r2 < R.r02_lo) inside = true;
+        else if (r2 > R.r02_hi) inside = false;
+        else {
+          if (dexact < 0) dexact = exact_dist<D>(s, a, m, j);
+          inside = dexact < R.r0;
+        }
+        if (inside) cw[r >> 1] += 1u << (16 * (r & 1));
+      }
+    };
+    if (cnt <= a.W) {
+      for (int e = lane; e < cnt; e += 32) count(gather<D>(a, a.nbr[ell_index<TPP>(e, m, a.npad)]));
+    } else {
+      row_scan<D, 32>(s, a, m, lane, [&](int, int v) { count(gather<D>(a, v)); });
+    }
+#pragma unroll
+    for (int w = 0; w < 4; w++) cw[w] = __reduce_add_sync(0xffffffffu, cw[w]);
+  }
+  return lane == 0 ? react_decide<D>(s, rx, a, pid, tm, cw) : tm;
+}
+
+// Global cell index of sorted particle i (its cell at the last rebuild).
+template <int D>
+__device__ inline int global_cell(const SysDev& s, const Args& a, int i) {
+  int g = 0, mult = 1;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    g += cell_coord(s, k, a.xr[k][i]) * mult;
+    mult *= s.nc[k];
+  }
+  return s.c0 + g;
+}
+
+// True if a cell of the 3^D stencil around particle m's cell lies in the
+// global cell range [cf, cl].  Lists are built from the same stencils, so a
+// particle of a CTA whose cells span [cf, cl] can have m in its list only
+// if this holds (and m itself lies in that CTA only if it holds).
+template <int D>
+__device__ inline bool stencil_meets(const SysDev& s, const Args& a, int m, int cf, int cl) {
+  int c[3] = {0, 0, 0};
+#pragma unroll
+  for (int k = 0; k < D; k++) c[k] = cell_coord(s, k, a.xr[k][m]);
+  constexpr int NROW = D == 3 ? 9 : (D == 2 ? 3 : 1);
+  const int h1 = D > 1 ? s.halo[1] : 0;
+  const int h2 = D > 2 ? s.halo[2] : 0;
+  bool hit = false;
+#pragma unroll
+  for (int q = 0; q < NROW; q++) {
+    const int dz = D == 3 ? q / 3 - 1 : 0;
+    const int dy = D >= 2 ? q % 3 - 1 : 0;
+    int row, lo0, hi0, lo1, hi1;
+    if (!(dy >= -h1 && dy <= h1 && dz >= -h2 && dz <= h2 &&
+          row_runs<D>(s, c, dy, dz, row, lo0, hi0, lo1, hi1)))
+      continue;
+    const int g0 = s.c0 + row;
+    hit = hit || (g0 + lo0 <= cl && g0 + hi0 >= cf) ||
+          (hi1 >= lo1 && g0 + lo1 <= cl && g0 + hi1 >= cf);
+  }
+  return hit;
+}
+
+// The merged reaction step of a drift kernel (F_RX_MERGED): every listed
+// particle of this step whose stencil meets the CTA's cells is resolved here,
+// a warp per particle, and its new meta word stored in rtype.  Several CTAs
+// may resolve the same particle; they compute and store the same word.  The
+// caller synchronises before reading rtype.
+template <int D, int TPP>
+__device__ __noinline__ void resolve_for_cta(const SysDev& s, const Args& a, const Chunk& ch, int n,
+                                       const int4* list) {
+  const int warp = (int)(threadIdx.x >> 5), l32 = (int)(threadIdx.x & 31);
+  const int cf = global_cell<D>(s, a, ch.beg), cl = global_cell<D>(s, a, ch.beg + ch.cnt - 1);
+  const int4 zero = make_int4(0, 0, 0, 0);
+  for (int b = warp * 32; b < n; b += LBLOCK) {
+    const int q = b + l32;
+    const int4 rec = q < n ? list[q] : zero;
+    const SysDev& sm = a.single ? s : a.sys[a.sid[rec.x]];
+    const bool rel = q < n && stencil_meets<D>(sm, a, rec.x, cf, cl);
+    unsigned int bal = __ballot_sync(0xffffffffu, rel);
+    while (bal) {
+      const int src = __ffs(bal) - 1;
+      bal &= bal - 1u;
+      int4 r;
+      r.x = __shfl_sync(0xffffffffu, rec.x, src);
+      r.y = __shfl_sync(0xffffffffu, rec.y, src);
+      r.z = __shfl_sync(0xffffffffu, rec.z, src);
+      r.w = __shfl_sync(0xffffffffu, rec.w, src);
+      const SysDev& sr = a.single ? s : a.sys[a.sid[r.x]];
+      const int newt = resolve_listed<D, TPP>(sr, a.rx + sr.rx0, a, r, l32);
+      if (l32 == 0) a.rtype[r.x] = (((uint32_t)r.y & ~RX_PENDING) & 0xffffff00u) | (uint32_t)newt;
     }
   }
 }
@@ -527,10 +648,17 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   uint32_t xo[3] = {0u, 0u, 0u};
 #pragma unroll
   for (int k = 0; k < D; k++) xo[k] = a.xp[k][i];
-  const uint32_t mi = a.meta[i];
+  uint32_t mi = a.meta[i];
+  const bool merged = (a.flags & F_RX_MERGED) != 0;
+  const int nrx = merged ? a.rx_count[rx_slot(eff_step(a))] : 0;
   prefetch_rows<TPP>(a, ch, cnt, active);
   __syncthreads();
   const SysDev& s = sh.sys;
+  if (nrx > 0) {  // this step's listed reaction draws (uniform over the CTA)
+    resolve_for_cta<D, TPP>(s, a, ch, nrx, a.rx_list + (size_t)rx_slot(eff_step(a)) * a.npad);
+    __syncthreads();
+    if (mi & RX_PENDING) mi = a.rtype[i];
+  }
   float acc[3] = {0.f, 0.f, 0.f};
   if (active && s.R2 > 0.f) {
     const int ti = mi & 0xff;
@@ -538,7 +666,8 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
       if (nb.v < 0) return;  // same molecule: reactions only
       int d[3];
       const float r2 = pair_geom<D>(s, nb.x, xo, d);
-      const int tj = nb.m & 0xff;
+      // a neighbour listed for this step's reaction: its new type
+      const int tj = (nb.m & RX_PENDING) ? (int)(a.rtype[nb.v] & 0xff) : (int)(nb.m & 0xff);
       if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
       const unsigned int pp = s.ppair[ti * MAXT + tj];
       const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
@@ -574,7 +703,8 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     float accb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < D; k++) accb[k] = sacc[k][tid];
-    const uint32_t mb = a.meta[ib];
+    uint32_t mb = a.meta[ib];
+    if (mb & RX_PENDING) mb = a.rtype[ib];  // resolved above (merged step)
     const int pid = a.pid[ib];
     // one Philox call for the next step's noise and reaction uniform
     const bool words = (a.flags & F_RX_NEXT) ||
@@ -583,26 +713,29 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     if (words) w0 = noise_words(s.seed, eff_em_step(a), pid, 0u);
     force_tail<D>(s, sh.walls, a, ib, pid, xb, mb, accb, words ? &w0 : nullptr);
     if (a.flags & F_RX_NEXT) {
-      a.meta_out[ib] = mb;  // the next step's types, unless its draw succeeds
       rec = make_int4(ib, (int)mb, a.ncnt[ib], pid);
       listed = rx_may_react<D>(s, (int)(mb & 0xff), rec.z, pid, eff_em_step(a), &w0);
     }
+    // the next step's types, unless its draw succeeds (then pending when the
+    // next drift kernel resolves it)
+    if (a.flags & (F_RX_NEXT | F_RX_MERGED))
+      a.meta_out[ib] = (listed && (a.flags & F_RX_FLAG)) ? (mb | RX_PENDING) : mb;
   }
   if (a.flags & F_RX_NEXT) {
     // append the particles whose draw may succeed (warp-aggregated)
     const unsigned int bal = __ballot_sync(0xffffffffu, listed);
     if (bal) {
       const int lane32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
-      const int p = (int)(eff_em_step(a) & 1);
+      const int p = rx_slot(eff_em_step(a));
       int base = 0;
       if (lane32 == leader) base = atomicAdd(a.rx_count + p, __popc(bal));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (listed) a.rx_list[(size_t)p * a.npad + base + __popc(bal & ((1u << lane32) - 1u))] = rec;
     }
   }
-  // the list of this step's parity was consumed by the reaction kernel that
-  // ran before this one: empty it for the next drift kernel
-  if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[eff_step(a) & 1] = 0;
+  // the slot of two steps ago was consumed before this kernel: empty it for
+  // the drift kernel (or list builder) of the next step that appends to it
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[rx_slot(eff_step(a) + 2)] = 0;
 }
 
 // Reaction kernel.  Phase A: TPP lanes per particle count, for every
@@ -684,12 +817,12 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   }
 }
 
-// Reaction kernel of the steps the previous drift kernel prefiltered: that
-// kernel copied every type forward and listed the particles whose draw may
-// succeed; one warp per listed particle counts its neighbours over its list
-// (lanes over entries) and lane 0 forms the propensities and draws
-// (pyrdsim.pyx:2070-2223).  A single system's tables are staged in shared
-// memory; a batch's are read through L1.
+// Reaction kernel of the steps the previous drift kernel (or the list
+// builder) prefiltered: that kernel copied every type forward and listed the
+// particles whose draw may succeed; one warp per listed particle resolves it
+// (resolve_listed) and writes its new type (pyrdsim.pyx:2070-2223).  A
+// single system's tables are staged in shared memory; a batch's are read
+// through L1.
 template <int D, int TPP>
 __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
   __shared__ SysDev sys1;
@@ -706,68 +839,30 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
     lr.store(reinterpret_cast<int*>(rx1), nr);
   }
   pdl_wait();
-  // the step counter, both parities' counts and this warp's first record of
-  // each parity are loaded together (one round trip instead of three)
+  // the step counter, the three slots' counts and this warp's first record
+  // of each slot are loaded together (one round trip instead of three)
   const int w0 = (int)((blockIdx.x * LBLOCK + threadIdx.x) >> 5);
-  const int n0 = a.rx_count[0], n1 = a.rx_count[1];
+  int nc[3];
+  int4 f[3];
   const int4 zero = make_int4(0, 0, 0, 0);
-  const int4 f0 = w0 < a.npad ? a.rx_list[w0] : zero;
-  const int4 f1 = w0 < a.npad ? a.rx_list[(size_t)a.npad + w0] : zero;
-  const int p = (int)(eff_step(a) & 1);
-  const int n = p ? n1 : n0;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    nc[q] = a.rx_count[q];
+    f[q] = w0 < a.npad ? a.rx_list[(size_t)q * a.npad + w0] : zero;
+  }
+  const int p = rx_slot(eff_step(a));
+  const int n = p == 0 ? nc[0] : (p == 1 ? nc[1] : nc[2]);
+  const int4 first = p == 0 ? f[0] : (p == 1 ? f[1] : f[2]);
   __syncthreads();
   const int4* list = a.rx_list + (size_t)p * a.npad;
   const int lane = threadIdx.x & 31;
   const int nwarps = (int)(gridDim.x * LBLOCK / 32);
   for (int q = w0; q < n; q += nwarps) {
-    const int4 rec = q == w0 ? (p ? f1 : f0) : list[q];
-    const int m = rec.x, cnt = rec.z, pid = rec.w;
-    const uint32_t mm = (uint32_t)rec.y;
-    const SysDev& s = a.single ? sys1 : a.sys[a.sid[m]];
+    const int4 rec = q == w0 ? first : list[q];
+    const SysDev& s = a.single ? sys1 : a.sys[a.sid[rec.x]];
     const RxDev* rx = a.single ? rx1 : a.rx + s.rx0;
-    const int tm = mm & 0xff;
-    uint32_t cw[4] = {0u, 0u, 0u, 0u};
-    if ((s.rx_nb_mask >> tm) & 1) {
-      uint32_t xm[3] = {0u, 0u, 0u};
-#pragma unroll
-      for (int k = 0; k < D; k++) xm[k] = a.xp[k][m];
-      const float Rrx2 = s.Rrx2;
-      auto count = [&](int v, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t mj) {
-        const int j = v & 0x7fffffff;
-        const uint32_t xj[3] = {x0, x1, x2};
-        int d[3];
-        const float r2 = pair_geom<D>(s, xj, xm, d);
-        if (!(r2 < Rrx2)) return;
-        const unsigned int rmask = s.rxmatch[tm * MAXT + (mj & 0xff)];
-        double dexact = -1.0;
-        for (unsigned int b = rmask; b; b &= b - 1u) {
-          const int r = __ffs(b) - 1;
-          const RxDev& R = rx[r];
-          bool inside;
-          if (r2 < R.r02_lo) inside = true;
-          else if (r2 > R.r02_hi) inside = false;
-          else {
-            if (dexact < 0) dexact = exact_dist<D>(s, a, m, j);
-            inside = dexact < R.r0;
-          }
-          if (inside) cw[r >> 1] += 1u << (16 * (r & 1));
-        }
-      };
-      if (cnt <= a.W) {
-        for (int e = lane; e < cnt; e += 32) {
-          const Nb nb = gather<D>(a, a.nbr[ell_index<TPP>(e, m, a.npad)]);
-          count(nb.v, nb.x[0], nb.x[1], nb.x[2], nb.m);
-        }
-      } else {
-        row_scan<D, 32>(s, a, m, lane, [&](int, int v) {
-          const Nb nb = gather<D>(a, v);
-          count(nb.v, nb.x[0], nb.x[1], nb.x[2], nb.m);
-        });
-      }
-#pragma unroll
-      for (int w = 0; w < 4; w++) cw[w] = __reduce_add_sync(0xffffffffu, cw[w]);
-    }
-    if (lane == 0) react_tail<D>(s, rx, a, m, pid, mm, cw);
+    const int newt = resolve_listed<D, TPP>(s, rx, a, rec, lane);
+    if (lane == 0) a.meta_out[rec.x] = ((uint32_t)rec.y & 0xffffff00u) | (uint32_t)newt;
   }
 }
 
