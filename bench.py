@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-precision", action="store_true")
+    p.add_argument("--no-sweep", action="store_true")
     return p.parse_args()
 
 
@@ -274,99 +275,215 @@ def force_error(eng, sd, device):
     return {"norm": norm, "per_particle_rms_floor": per}
 
 
-def precision_report(local):
-    """Force error against float64 for every configuration's shape after 200
-    thermalising steps (the patchy colloids start with every bond at rest,
-    where the relative error of near-zero bond forces says nothing), and the
-    trajectory error of the reaction-free LJ fluid after 100 steps with the
-    same injected normals (float64 PyTorch integration)."""
-    import numpy as np
+def _events_ms(stream_ptrs, fn):
+    """Run fn() between CUDA events recorded on the first and last of the
+    engines' streams (fn synchronises each engine it steps); device ms."""
     import torch
+    s0 = torch.cuda.ExternalStream(stream_ptrs[0])
+    s1 = torch.cuda.ExternalStream(stream_ptrs[-1])
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(s0)
+    fn()
+    b.record(s1)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b)
+
+
+def trajectory_error(sds, local, steps=100, seed=11):
+    """Positions after ``steps`` injected-noise steps of the float32 engine
+    against the float64 engine (precision="float64", pinned to the oracle at
+    1e-12 by the GPU tests) from the same thermalised state; the uniforms are
+    1 so that no reaction fires.  Max absolute and relative differences."""
+    import numpy as np
+    from pyrdsim_gb300.engine import Engine
+    f32 = Engine(sds, device=local)
+    f32.step(200)
+    x0, t0 = f32.state()
+    f64 = Engine(sds, device=local, precision="float64")
+    f64.set_state(x0, t0)
+    f32.set_state(x0, t0)
+    n, D = f32.N, f32.D
+    rng = np.random.default_rng(seed)
+    ones = np.ones((10, n))
+    for c in range(steps // 10):
+        xi = rng.standard_normal((10, n, D))
+        f32.step(10, xi=xi, u1=ones, u2=ones)
+        f64.step(10, xi=xi, u1=ones, u2=ones)
+    xa, _ = f32.state()
+    xb, _ = f64.state()
+    d = xa - xb
+    off = 0
+    for sd in sds:
+        m = sd.model
+        sl = slice(off, off + sd.n_particles)
+        for k in range(D):
+            if m.periodic[k] > 0:
+                d[sl, k] -= m.L[k] * np.round(d[sl, k] / m.L[k])
+        off += sd.n_particles
+    f32.close()
+    f64.close()
+    return {"max_abs": float(np.abs(d).max()),
+            "max_rel": float((np.abs(d) / np.maximum(np.abs(xb), 1.0)).max()),
+            "steps": steps}
+
+
+def precision_report(local):
+    """For every configuration's shape: the float32 drift against the plain
+    PyTorch float64 drift after 200 thermalising steps (the patchy colloids
+    start with every bond at rest), and positions after 100 injected-noise
+    steps against the float64 engine."""
     from pyrdsim_gb300 import workloads
     from pyrdsim_gb300.engine import Engine
     dev = f"cuda:{local}"
     out = {}
     cases = {
-        "cfg1_lj_fluid_n1024": workloads.lj_fluid(n=1024),
-        "cfg3_patchy_colloids_n65536": workloads.patchy_colloids(n_molecules=16384),
-        "cfg4_ensemble_8_systems": None,
+        "cfg1_lj_fluid_n1024": [workloads.lj_fluid(n=1024)],
+        "cfg2_active_wall_fluid_n65536": [workloads.active_wall_fluid(n=65536)],
+        "cfg3_patchy_colloids_n65536": [workloads.patchy_colloids(n_molecules=16384)],
+        "cfg4_ensemble_8_systems": workloads.ensemble(n_systems=8, seed=4),
     }
-    for name, sd in cases.items():
-        if sd is None:
-            errs = []
-            for e in workloads.ensemble(n_systems=8, seed=4):
-                eng = Engine([e], device=local)
-                eng.step(200)
-                errs.append(force_error(eng, e, dev))
-            out[name] = {"norm": max(q["norm"] for q in errs),
-                         "per_particle_rms_floor": max(q["per_particle_rms_floor"] for q in errs)}
-        else:
+    for name, sds in cases.items():
+        errs = []
+        for sd in sds:
             eng = Engine([sd], device=local)
             eng.step(200)
-            out[name] = force_error(eng, sd, dev)
-    # trajectory: 100 steps of the LJ fluid, noise injected into both
-    sd = workloads.lj_fluid(n=1024)
-    eng = Engine([sd], device=local)
-    x0, t0 = eng.state()
-    rng = np.random.default_rng(11)
-    xi = rng.standard_normal((100, sd.n_particles, 2))
-    eng.step(100, xi=xi, u1=np.ones((100, sd.n_particles)), u2=np.ones((100, sd.n_particles)))
-    xg, _ = eng.state()
-    m = sd.model
-    L = np.asarray(m.L, dtype=float)[:2]
-    D_t = float(m.tau_by_tauD[0])
-    x = x0.copy()
-    for k in range(100):
-        a = fp64_drift(sd, x, t0, dev)
-        x = x + m.dt * D_t * a
-        x = x + np.sqrt(2.0 * m.dt * D_t) * xi[k]
-        x = np.mod(x, L)
-    d = xg - x
-    d -= L * np.round(d / L)
-    out["cfg1_lj_fluid_n1024_positions_after_100_steps"] = {
-        "max_abs": float(np.abs(d).max()),
-        "max_rel": float((np.abs(d) / np.maximum(np.abs(x), 1.0)).max())}
+            errs.append(force_error(eng, sd, dev))
+            eng.close()
+        row = {"force_norm": max(q["norm"] for q in errs),
+               "force_per_particle_rms_floor": max(q["per_particle_rms_floor"] for q in errs)}
+        try:
+            row["positions_after_100_steps"] = trajectory_error(sds, local)
+        except Exception as exc:
+            row["positions_after_100_steps"] = {"unavailable": str(exc)[:200]}
+        out[name] = row
     return out
 
 
-def ensemble_comparison(local, steps=100, n_systems=512):
-    """Batched ensemble (all systems in one handle, one launch per kernel per
-    step) vs the plain per-system form (one handle per system, stepped one
-    system at a time), both on the GPU with Philox noise."""
-    import torch
+def ensemble_comparison(local, steps=5000, n_systems=512, f64_sample=64):
+    """The 512-system ensemble: batched (all systems in one handle, autotuned
+    geometry) against the plain per-system form (one handle per system,
+    stepped one system at a time) with the default and with the autotuned
+    geometry, all over the configuration's 5,000 steps with Philox noise,
+    timed with CUDA events on the engines' streams; and the plain form in
+    float64 (the reference's precision) on every (512 / f64_sample)-th
+    system, scaled by particles.  Rebuild periods replay as CUDA graphs of
+    neighbor_list_update_frequency (10) steps: a graph of 100 steps would
+    hold 10 rebuild periods and change nothing but the launch of the graph
+    itself (one launch per ten steps here)."""
     from pyrdsim_gb300 import workloads
     from pyrdsim_gb300.engine import Engine
     from pyrdsim_gb300.autotune import autotune
     sds = workloads.ensemble(n_systems=n_systems)
     total = sum(s.n_particles for s in sds)
-    tuned = autotune(sds, device=local, steps=steps)
-    batch = Engine(sds, device=local, skin=tuned["skin"],
-                   threads_per_particle=tuned["threads_per_particle"] or 0)
-    batch.step(steps // 2)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    batch.step(steps)
-    torch.cuda.synchronize()
-    t_b = time.perf_counter() - t0
+    tuned = autotune(sds, device=local, steps=100)
+    tpp = tuned["threads_per_particle"] or 0
+    out = {"n_systems": n_systems, "n_particles": total, "steps": steps, "unit": UNIT,
+           "batched_options": tuned,
+           "workload": "512 systems, N log-uniform [256, 16384], density U[0.2, 0.7], "
+                       "kT U[0.5, 2], LJ or Yukawa, half with two-state reactions"}
+    clocks = ClockSampler(local)
+    batch = Engine(sds, device=local, skin=tuned["skin"], threads_per_particle=tpp)
+    batch.step(100)
+    ms = _events_ms([batch.stream()], lambda: batch.step(steps))
     batch.close()
-    engines = [Engine([s], device=local) for s in sds]
+    out["batched"] = total * steps / (ms / 1e3)
+    for label, kw in (("plain_per_system", {}),
+                      ("plain_per_system_autotuned", {"skin": tuned["skin"],
+                                                      "threads_per_particle": tpp})):
+        engines = [Engine([s], device=local, **kw) for s in sds]
+        for e in engines:
+            e.step(20)
+        ms = _events_ms([e.stream() for e in engines],
+                        lambda: [e.step(steps) for e in engines])
+        for e in engines:
+            e.close()
+        out[label] = total * steps / (ms / 1e3)
+    sample = sds[::max(1, n_systems // f64_sample)]
+    engines = [Engine([s], device=local, precision="float64") for s in sample]
     for e in engines:
-        e.step(steps // 2)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for e in engines:
-        e.step(steps)
-    torch.cuda.synchronize()
-    t_p = time.perf_counter() - t0
+        e.step(20)
+    ms = _events_ms([e.stream() for e in engines], lambda: [e.step(steps) for e in engines])
     for e in engines:
         e.close()
-    b = total * steps / t_b
-    p = total * steps / t_p
-    return {"n_systems": n_systems, "n_particles": total, "steps": steps,
-            "batched": b, "plain_per_system": p, "speedup": b / p, "unit": UNIT,
-            "batched_options": tuned,
-            "workload": "512 systems, N log-uniform [256, 16384], density U[0.2, 0.7], "
-                        "kT U[0.5, 2], LJ or Yukawa, half with two-state reactions"}
+    out["plain_per_system_float64"] = sum(s.n_particles for s in sample) * steps / (ms / 1e3)
+    out["plain_float64_sample"] = f"{len(sample)} of {n_systems} systems (every " \
+                                  f"{max(1, n_systems // f64_sample)}th), {steps} steps"
+    out["speedup"] = out["batched"] / out["plain_per_system"]
+    out["speedup_vs_autotuned_plain"] = out["batched"] / out["plain_per_system_autotuned"]
+    out["speedup_vs_float64_plain"] = out["batched"] / out["plain_per_system_float64"]
+    out["clocks"] = clocks.stop()
+    try:
+        errs = [force_error_of(sd, local) for sd in sds[::64]]
+        out["force_err_vs_fp64_batched_geometry"] = {
+            "norm": max(q["norm"] for q in errs),
+            "per_particle_rms_floor": max(q["per_particle_rms_floor"] for q in errs),
+            "systems": len(errs)}
+    except Exception as exc:
+        out["force_err_vs_fp64_batched_geometry"] = {"unavailable": str(exc)[:200]}
+    return out
+
+
+def force_error_of(sd, local):
+    from pyrdsim_gb300.engine import Engine
+    eng = Engine([sd], device=local)
+    eng.step(200)
+    r = force_error(eng, sd, f"cuda:{local}")
+    eng.close()
+    return r
+
+
+def lj_fluid_plain_method(local, steps=10000):
+    """The 2D LJ fluid (N = 1,024, density 0.5, relaxed uniform start) over
+    its stated 10,000 steps with the float64 plain method and with the
+    float32 forces; CUDA events on the engine stream."""
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    sd = workloads.lj_fluid(n=1024)
+    out = {"workload": "2D LJ fluid, N=1024, density 0.5, dt=1e-4, relaxed uniform start",
+           "steps": steps, "unit": UNIT}
+    for prec in ("float64", "float32"):
+        eng = Engine([sd], device=local, precision=prec)
+        eng.step(100)
+        ms = _events_ms([eng.stream()], lambda: eng.step(steps))
+        out[prec] = sd.n_particles * steps / (ms / 1e3)
+        eng.close()
+    return out
+
+
+def n_sweep(local, sizes=((65536, 1000), (1048576, 200), (4194304, 100))):
+    """The active wall fluid at growing N (density 0.4): throughput and the
+    drift kernel's average launch span (device timestamps of the timed
+    replays) against the measured HBM peak.  At 65,536 particles the state
+    (~25 MB) lives in L2; at 4M (~1.5 GB) it cannot."""
+    from pyrdsim_gb300 import workloads
+    from pyrdsim_gb300.engine import Engine
+    import torch
+    peak, _ = peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    rows = []
+    for n, steps in sizes:
+        sd = workloads.active_wall_fluid(n=n)
+        eng = Engine([sd], device=local)
+        eng.set_profiling(False, stamps=True)
+        eng.step(steps)
+        eng.profile()
+        flush.zero_()
+        ms = _events_ms([eng.stream()], lambda: eng.step(steps))
+        prof = eng.profile()
+        span = prof["drift_span"]
+        us = 1e3 * span["ms"] / max(1, span["launches"])
+        ach = ALG_BYTES * n / (us / 1e6) / 1e9
+        rows.append({"n_particles": n, "steps": steps,
+                     "particle_steps_per_s": n * steps / (ms / 1e3),
+                     "us_per_step": 1e3 * ms / steps,
+                     "drift_span_us": us, "drift_achieved_gbs": ach,
+                     "drift_frac_of_measured_hbm": ach / peak,
+                     "device_bytes": eng.info()["device_bytes"]})
+        eng.close()
+        del sd
+    return rows
 
 
 def adjoint_timing(local, n=16384, steps=1000, loss_steps=500, every=32, reps=2):
@@ -406,13 +523,14 @@ def adjoint_timing(local, n=16384, steps=1000, loss_steps=500, every=32, reps=2)
 
 
 def run_ours(args, rank, ws, local):
-    import numpy as np
     import torch
     from pyrdsim_gb300 import workloads
     from pyrdsim_gb300.engine import Engine
     torch.cuda.set_device(local)
     sd = workloads.active_wall_fluid(n=args.n, seed=2 + rank)
     eng = Engine([sd], device=local)
+    # the drift kernel stamps each CTA's start and end in the timed replays
+    eng.set_profiling(False, stamps=True)
     N, seg = sd.n_particles, args.segment
     stream = torch.cuda.ExternalStream(eng.stream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
@@ -420,7 +538,7 @@ def run_ours(args, rank, ws, local):
     for _ in range(args.warmup):
         eng.step(seg)
     torch.cuda.synchronize()
-    eng.profile()  # reset counters
+    eng.profile()  # reset counters and stamps
     barrier(ws)
     clocks = ClockSampler(local) if rank == 0 else None
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -435,25 +553,24 @@ def run_ours(args, rank, ws, local):
     torch.cuda.synchronize()
     barrier(ws)
     clk = clocks.stop() if clocks else None
-    prof_counts = eng.profile()
+    timed = eng.profile()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     ms_max = max_over_ranks(ms, ws)
     value = ws * N * seg * args.steps / (ms_max / 1e3)
-    launches = sum(v["launches"] for k, v in prof_counts.items() if k != "hook")
-    # roofline pass: per-kernel CUDA events on the engine stream
-    eng.set_profiling(True)
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
+    launches = sum(v["launches"] for k, v in timed.items() if k not in ("hook", "drift_span"))
+    span = timed["drift_span"]
+    span_us = 1e3 * span["ms"] / max(1, span["launches"])
+    peak, peak_kind = peaks()
+    achieved = ALG_BYTES * N / (span_us / 1e6) / 1e9
+    traffic = traffic_per_launch(N)
+    # a short serialised pass (CUDA events around every launch; no graphs)
+    # for the per-class split; not the timed pass
+    eng.set_profiling(True, stamps=False)
+    for k in range(2):
         eng.step(seg)
     torch.cuda.synchronize()
-    prof = eng.profile()
+    ser = eng.profile()
     eng.set_profiling(False)
-    f_ms = prof["force"]["ms"] / max(1, prof["force"]["timed"])
-    r_ms = prof["react"]["ms"] / max(1, prof["react"]["timed"])
-    peak, peak_kind = peaks()
-    achieved = ALG_BYTES * N / (f_ms / 1e3) / 1e9
-    traffic = traffic_per_launch(N)
     # end to end through the C ABI with host buffers: state in, segment, state out
     xh = torch.empty((N, 2), dtype=torch.float64, pin_memory=True).numpy()
     th = torch.empty((N,), dtype=torch.int32, pin_memory=True).numpy()
@@ -489,10 +606,14 @@ def run_ours(args, rank, ws, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "kernel": "k_force_l<2,2>",
                      "algorithmic_bytes_per_launch": ALG_BYTES * N,
-                     "avg_launch_us": f_ms * 1e3, "peak_source": peak_kind,
-                     "react_avg_launch_us": r_ms * 1e3},
-        "kernel_ms": {k: v["ms"] for k, v in prof.items()},
-        "kernel_launches": {k: v["launches"] for k, v in prof.items()},
+                     "avg_launch_us": span_us, "launches_timed": span["launches"],
+                     "timing": "device global-timer stamps in the timed graph replays: last "
+                               "CTA end minus first CTA start, averaged over the launches",
+                     "peak_source": peak_kind,
+                     "drift_share_of_timed": span["ms"] / ms},
+        "kernel_launches": {k: v["launches"] for k, v in timed.items() if k != "drift_span"},
+        "serialised_kernel_us": {k: 1e3 * v["ms"] / max(1, v["timed"])
+                                 for k, v in ser.items() if k != "drift_span" and v["timed"]},
         "clocks": clk,
         "engine": eng.info(),
     }
@@ -505,22 +626,20 @@ def run_ours(args, rank, ws, local):
             out["force_err_vs_fp64"] = force_error(eng, sd, f"cuda:{local}")
         except Exception as exc:
             out["force_err_vs_fp64"] = {"unavailable": str(exc)[:200]}
-    if rank == 0 and ws == 1 and not args.no_ensemble:
-        eng.close()
-        try:
-            out["ensemble"] = ensemble_comparison(local)
-        except Exception as exc:
-            out["ensemble"] = {"unavailable": str(exc)[:200]}
-    if rank == 0 and ws == 1 and not args.no_precision:
-        try:
-            out["precision_vs_fp64"] = precision_report(local)
-        except Exception as exc:
-            out["precision_vs_fp64"] = {"unavailable": str(exc)[:200]}
-    if rank == 0 and ws == 1 and not args.no_adjoint:
-        try:
-            out["adjoint"] = adjoint_timing(local)
-        except Exception as exc:
-            out["adjoint"] = {"unavailable": str(exc)[:200]}
+    eng.close()
+    extras = [("precision_vs_fp64", args.no_precision, precision_report),
+              ("lj_fluid_plain_method", args.no_precision, lj_fluid_plain_method),
+              ("ensemble", args.no_ensemble, ensemble_comparison),
+              ("n_sweep", args.no_sweep, n_sweep),
+              ("adjoint", args.no_adjoint, adjoint_timing)]
+    if rank == 0 and ws == 1:
+        for key, skip, fn in extras:
+            if skip:
+                continue
+            try:
+                out[key] = fn(local)
+            except Exception as exc:
+                out[key] = {"unavailable": str(exc)[:200]}
     if rank == 0:
         print(json.dumps(out))
 

@@ -318,16 +318,23 @@ typedef struct {
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 
 /* Kernel accounting (no reference counterpart; measurement only).  Launch
- * counts are always kept; with profiling enabled every kernel launch is also
+ * counts are always kept.  With bit 0 of `enable` every kernel launch is also
  * bracketed by CUDA events on the handle's stream and its device time summed
  * per class: 0 = drift (k_force_l), 1 = reactions (k_react_l,
  * k_react_listed), 2 = stand-alone Euler-Maruyama (k_em), 3 = cell-list and
- * Verlet-list rebuild (6 kernels), 4 = hooks and observables. */
+ * Verlet-list rebuild (6 kernels), 4 = hooks and observables (the events
+ * serialise launches and keep graphs from replaying).  With bit 1 the drift
+ * kernel itself records the global timer when each CTA starts its work
+ * (after waiting for the previous kernel) and ends it; drift_span_ms sums,
+ * per launch, last end minus first start over the last drift_spans launches
+ * (up to 32768 kept), without changing how the step runs (graphs replay). */
 #define RDSIM_PROFILE_CLASSES 5
 typedef struct {
   int64_t launches[RDSIM_PROFILE_CLASSES];
   double ms[RDSIM_PROFILE_CLASSES];
   int64_t timed[RDSIM_PROFILE_CLASSES];
+  double drift_span_ms;
+  int64_t drift_spans;
 } rdsim_profile;
 int rdsim_set_profiling(rdsim_handle* h, int32_t enable);
 /* Fills *p and resets the counters (synchronises the stream). */

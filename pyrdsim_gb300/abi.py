@@ -147,7 +147,8 @@ PROFILE_NAMES = ["force", "react", "em", "rebuild", "hook"]
 class Profile(C.Structure):
     _fields_ = [("launches", C.c_int64 * PROFILE_CLASSES),
                 ("ms", C.c_double * PROFILE_CLASSES),
-                ("timed", C.c_int64 * PROFILE_CLASSES)]
+                ("timed", C.c_int64 * PROFILE_CLASSES),
+                ("drift_span_ms", C.c_double), ("drift_spans", C.c_int64)]
 
 
 def dptr(a):

@@ -199,7 +199,17 @@ struct Args {
   Chunk chunk1;                   // ... with these table offsets
   int n_total;
   int flags;
+  // drift-kernel timestamps (measurement): [ring][CTAs][2] global-timer
+  // values of each CTA's start and end, slot = step mod ring
+  unsigned long long* stamps;
+  int stamp_ring;
 };
+
+__device__ inline unsigned long long global_timer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 enum : int {
   F_STORE_DRIFT = 1,              // write the drift (sorted order)

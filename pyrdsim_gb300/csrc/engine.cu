@@ -169,6 +169,11 @@ struct rdsim_handle {
   std::vector<Pend> pending;
   std::vector<cudaEvent_t> ev_pool;
   double prof_ms[RDSIM_PROFILE_CLASSES] = {};
+  // drift-kernel timestamps (rdsim_set_profiling bit 1)
+  bool stamp_on = false;
+  unsigned long long* stamps = nullptr;   // [ring][CTAs][2]
+  unsigned long long* stamp_sum = nullptr;  // [2]: span sum (ns), launches
+  int stamp_ring = 0;
   int64_t prof_n[RDSIM_PROFILE_CLASSES] = {};
 };
 
@@ -267,6 +272,10 @@ Args make_args(rdsim_handle* h) {
   a.sid = h->sid;
   a.npad = h->npad;
   a.single = h->nsys == 1 ? 1 : 0;
+  if (h->stamp_on) {
+    a.stamps = h->stamps;
+    a.stamp_ring = h->stamp_ring;
+  }
   if (!h->chunks_h.empty()) a.chunk1 = h->chunks_h[0];
   return a;
 }
@@ -587,6 +596,8 @@ void free_all(rdsim_handle* h) {
   F(h->inj_xi); F(h->inj_u1); F(h->inj_u2); F(h->traj_x); F(h->traj_t);
   F(h->olaws_d); F(h->owalls_d); F(h->oterms_d); F(h->obs_part); F(h->obs_counts);
   F(h->rdf_counts);
+  F(h->stamps);
+  F(h->stamp_sum);
   for (auto& p : h->pending) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -1675,7 +1686,26 @@ int rdsim_get_stream(rdsim_handle* h, void** stream) {
 
 int rdsim_set_profiling(rdsim_handle* h, int32_t enable) {
   if (!h) return fail(RDSIM_ERR_ARG, "null handle");
-  h->prof = enable != 0;
+  CK(cudaSetDevice(h->device));
+  h->prof = (enable & 1) != 0;
+  const bool stamp = (enable & 2) != 0;
+  if (stamp != h->stamp_on) {
+    // captured graphs hold the kernels' arguments: capture them again
+    CK(cudaStreamSynchronize(h->stream));
+    for (auto& g : h->graph_cache) cudaGraphExecDestroy(g.second.exec);
+    h->graph_cache.clear();
+    h->stamp_on = stamp;
+  }
+  if (stamp && !h->stamps) {
+    const size_t nctas = std::max<size_t>(1, h->chunks_h.size());
+    const size_t ring = std::min<size_t>(32768, std::max<size_t>(64, (512u << 20) / (16 * nctas)));
+    int64_t dummy = 0;
+    int rc;
+    if ((rc = dalloc(&h->stamps, ring * nctas * 2, &dummy))) return rc;
+    if ((rc = dalloc(&h->stamp_sum, 2, &dummy))) return rc;
+    h->stamp_ring = (int)ring;
+    CK(cudaMemsetAsync(h->stamps, 0, sizeof(unsigned long long) * ring * nctas * 2, h->stream));
+  }
   return 0;
 }
 
@@ -1684,6 +1714,22 @@ int rdsim_get_profile(rdsim_handle* h, rdsim_profile* p) {
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   resolve_profile(h);
+  p->drift_span_ms = 0.0;
+  p->drift_spans = 0;
+  if (h->stamps) {
+    const int nctas = (int)std::max<size_t>(1, h->chunks_h.size());
+    CK(cudaMemsetAsync(h->stamp_sum, 0, 2 * sizeof(unsigned long long), h->stream));
+    k_stamp_spans<<<h->stamp_ring, 256, 0, h->stream>>>(h->stamps, h->stamp_ring, nctas,
+                                                        h->stamp_sum, h->stamp_sum + 1);
+    CK(cudaGetLastError());
+    unsigned long long r[2] = {0ull, 0ull};
+    CK(cudaMemcpyAsync(r, h->stamp_sum, sizeof r, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemsetAsync(h->stamps, 0,
+                       sizeof(unsigned long long) * (size_t)h->stamp_ring * nctas * 2, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    p->drift_span_ms = (double)r[0] * 1e-6;
+    p->drift_spans = (int64_t)r[1];
+  }
   for (int c = 0; c < RDSIM_PROFILE_CLASSES; c++) {
     p->launches[c] = h->nlaunch[c];
     p->ms[c] = h->prof_ms[c];

@@ -648,6 +648,8 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   uint32_t xo[3] = {0u, 0u, 0u};
 #pragma unroll
   for (int k = 0; k < D; k++) xo[k] = a.xp[k][i];
+  if (a.stamps && threadIdx.x == 0)
+    a.stamps[((size_t)(eff_step(a) % a.stamp_ring) * gridDim.x + blockIdx.x) * 2] = global_timer();
   uint32_t mi = a.meta[i];
   const bool merged = (a.flags & F_RX_MERGED) != 0;
   const int nrx = merged ? a.rx_count[rx_slot(eff_step(a))] : 0;
@@ -736,6 +738,48 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   // the slot of two steps ago was consumed before this kernel: empty it for
   // the drift kernel (or list builder) of the next step that appends to it
   if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[rx_slot(eff_step(a) + 2)] = 0;
+  if (a.stamps) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+      a.stamps[((size_t)(eff_step(a) % a.stamp_ring) * gridDim.x + blockIdx.x) * 2 + 1] =
+          global_timer();
+  }
+}
+
+// Spans of the stamped drift launches: per ring slot, the last CTA end minus
+// the first CTA start (slots never written are skipped), summed.
+static __global__ void k_stamp_spans(const unsigned long long* st, int ring, int nctas,
+                              unsigned long long* sum, unsigned long long* count) {
+  __shared__ unsigned long long lo[32], hi[32];
+  const int slot = blockIdx.x;
+  unsigned long long a0 = ~0ull, b0 = 0ull;
+  for (int c = threadIdx.x; c < nctas; c += blockDim.x) {
+    const unsigned long long s0 = st[((size_t)slot * nctas + c) * 2];
+    const unsigned long long e0 = st[((size_t)slot * nctas + c) * 2 + 1];
+    if (s0 && e0) {
+      a0 = min(a0, s0);
+      b0 = max(b0, e0);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a0 = min(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+    b0 = max(b0, __shfl_xor_sync(0xffffffffu, b0, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    lo[threadIdx.x >> 5] = a0;
+    hi[threadIdx.x >> 5] = b0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      a0 = min(a0, lo[w]);
+      b0 = max(b0, hi[w]);
+    }
+    if (b0 > a0) {
+      atomicAdd(sum, b0 - a0);
+      atomicAdd(count, 1ull);
+    }
+  }
 }
 
 // Reaction kernel.  Phase A: TPP lanes per particle count, for every

@@ -313,16 +313,22 @@ class Engine:
         _check(self.lib.rdsim_get_stream(self.h, C.byref(s)))
         return s.value
 
-    def set_profiling(self, on=True):
-        _check(self.lib.rdsim_set_profiling(self.h, 1 if on else 0))
+    def set_profiling(self, on=True, stamps=False):
+        """``on``: CUDA events around every launch (serialised, no graphs);
+        ``stamps``: the drift kernel records per-CTA start and end times
+        (graph replays unchanged; see :meth:`profile`)."""
+        _check(self.lib.rdsim_set_profiling(self.h, (1 if on else 0) | (2 if stamps else 0)))
 
     def profile(self):
         """Launch counts and event-timed device ms per kernel class since the
-        last call (resets the counters)."""
+        last call, and the drift kernel's summed start-to-end spans when
+        stamps are on ("drift_span": ms and launches); resets the counters."""
         p = abi.Profile()
         _check(self.lib.rdsim_get_profile(self.h, C.byref(p)))
-        return {name: {"launches": p.launches[c], "ms": p.ms[c], "timed": p.timed[c]}
-                for c, name in enumerate(abi.PROFILE_NAMES)}
+        out = {name: {"launches": p.launches[c], "ms": p.ms[c], "timed": p.timed[c]}
+               for c, name in enumerate(abi.PROFILE_NAMES)}
+        out["drift_span"] = {"ms": p.drift_span_ms, "launches": p.drift_spans}
+        return out
 
     def info(self):
         i = abi.Info()

@@ -1,10 +1,12 @@
 """Seeded synthetic systems with the shapes of the benchmark configurations.
 
 Each builder returns a :class:`pyrdsim_gb300.model.SystemData` (parameters in
-the reference's dictionary form plus an initial state).  Positions start on a
-jittered square lattice at the target density: uniform random placement would
+the reference's dictionary form plus an initial state).  The LJ fluid starts
+as its configuration states: uniform random positions relaxed by steepest
+descent until no pair is closer than 0.9 sigma.  The other workloads start on
+a jittered square lattice at the target density (uniform placement would
 overlap Lennard-Jones cores and blow the first step up, while a lattice with
-jitter below half the spacing keeps every pair beyond 0.9 sigma.
+jitter below half the spacing keeps every pair beyond 0.9 sigma).
 
 * ``lj_fluid``          -- 2D single-species LJ, periodic (N=1024, rho=0.5)
 * ``active_wall_fluid`` -- 2D two-species WCA/LJ with a 9-3 wall and
@@ -43,7 +45,42 @@ def _single_atoms(n):
     return mol, np.arange(n, dtype=np.int32)
 
 
-def lj_fluid(n=1024, rho=0.5, seed=1, dt=1e-4):
+def relaxed_uniform(n, L, rng, dmin=0.9, rc=2.5, cap=0.05, max_iter=20000):
+    """Uniform random positions in a periodic square box of side L, relaxed
+    by steepest descent on the Lennard-Jones energy (sigma = 1, epsilon = 1,
+    cut at rc; the reference's form with r0 = 2^(1/6)) until no pair is
+    closer than dmin.  Each iteration moves every particle along its force,
+    by at most ``cap`` (overlapping pairs carry huge forces), in float64 on
+    the host; seeded, so the start is reproducible."""
+    from scipy.spatial import cKDTree
+    x = rng.uniform(0.0, L, (n, 2))
+    for _ in range(max_iter):
+        pairs = cKDTree(x, boxsize=L).query_pairs(rc, output_type="ndarray")
+        if len(pairs) == 0:
+            break
+        i, j = pairs[:, 0], pairs[:, 1]
+        d = x[j] - x[i]
+        d -= L * np.round(d / L)
+        r = np.sqrt((d * d).sum(1))
+        if r.min() >= dmin:
+            break
+        r = np.maximum(r, 1e-6)
+        s6 = (WCA_R0 / r) ** 6
+        fr = -12.0 * s6 * (s6 - 1.0) / r / r  # f/r, a_i += f/r (x_j - x_i)
+        a = np.zeros_like(x)
+        np.add.at(a, i, fr[:, None] * d)
+        np.add.at(a, j, -fr[:, None] * d)
+        step = np.linalg.norm(a, axis=1)
+        scale = np.where(step > 0, np.minimum(1.0, cap / np.maximum(step, 1e-300)), 0.0)
+        x = np.mod(x + scale[:, None] * a, L)
+    return x
+
+
+def lj_fluid(n=1024, rho=0.5, seed=1, dt=1e-4, start="relaxed"):
+    """The 2D Lennard-Jones fluid.  ``start="relaxed"``: uniform random
+    positions relaxed by steepest descent until no pair is closer than 0.9
+    sigma (the configuration's stated start); ``"lattice"``: a jittered
+    square lattice."""
     rng = np.random.default_rng(seed)
     L = np.sqrt(n / rho)
     params = {
@@ -55,7 +92,7 @@ def lj_fluid(n=1024, rho=0.5, seed=1, dt=1e-4):
         "reactions": [],
     }
     m = model.Model.from_dict(params)
-    x = jittered_lattice(n, [L, L], rng)
+    x = relaxed_uniform(n, L, rng) if start == "relaxed" else jittered_lattice(n, [L, L], rng)
     mol, first = _single_atoms(n)
     return model.SystemData(m, x, np.zeros(n, np.int32), mol, first)
 
