@@ -156,13 +156,7 @@ typedef struct {
                                      may succeed (same results).  0: when few
                                      draws are expected to pass the bound;
                                      > 0: whenever the rates allow; < 0: off  */
-  int32_t react_in_drift;         /* 0: with the prefilter, the drift kernel
-                                     resolves the prefiltered reaction draws of
-                                     its own step inside graph-replayed
-                                     periods, and no reaction kernel runs
-                                     between rebuilds (same results); < 0: a
-                                     separate reaction kernel every step      */
-  int32_t reserved[4];
+  int32_t reserved[5];
 } rdsim_options;
 
 /* rdsim_step flags */
@@ -312,8 +306,6 @@ typedef struct {
   int64_t device_bytes;
   int32_t reaction_prefilter;     /* 1: on for this handle                    */
   int32_t force_precision;        /* as in rdsim_options                      */
-  int32_t react_in_drift;         /* 1: on for this handle                    */
-  int32_t pad;
 } rdsim_info;
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 

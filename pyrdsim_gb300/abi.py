@@ -109,8 +109,7 @@ class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("skin", C.c_double),
                 ("threads_per_particle", C.c_int32), ("force_precision", C.c_int32),
                 ("use_graphs", C.c_int32), ("list_width", C.c_int32),
-                ("reaction_prefilter", C.c_int32), ("react_in_drift", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("reaction_prefilter", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Info(C.Structure):
@@ -119,8 +118,7 @@ class Info(C.Structure):
                 ("list_width", C.c_int32), ("skin", C.c_double),
                 ("cell_size_min", C.c_double), ("interaction_range", C.c_double),
                 ("device_bytes", C.c_int64), ("reaction_prefilter", C.c_int32),
-                ("force_precision", C.c_int32), ("react_in_drift", C.c_int32),
-                ("pad", C.c_int32)]
+                ("force_precision", C.c_int32)]
 
 
 RDF_OTHER_MOLECULES = 1

@@ -192,8 +192,6 @@ struct Args {
                                   // may succeed at a step, in slot step % 3,
                                   // as {sorted index, meta, list entries, pid}
   int* rx_count;                  // [3]
-  uint32_t* rtype;                // per particle: meta word after this step's
-                                  // reaction (drift kernel with F_RX_MERGED)
   const int* sid;                 // system of each particle
   int single;                     // one system: chunks follow from blockIdx
   Chunk chunk1;                   // ... with these table offsets
@@ -221,22 +219,12 @@ enum : int {
   F_RX_NEXT = 64,                 // drift kernel: copy the types forward and
                                   // list the particles whose reaction draw of
                                   // the next step may succeed
-  F_RX_HERE = 128,                // list builder: the same for its own step
-  F_RX_MERGED = 256,              // drift kernel: first resolves this step's
-                                  // listed reaction draws itself (no reaction
-                                  // kernel ran), then writes every type
-  F_RX_FLAG = 512                 // drift kernel: mark the particles it lists
-                                  // (RX_PENDING) for a merged next step
+  F_RX_HERE = 128                 // list builder: the same for its own step
 };
 
-// Meta-word bit of a particle listed for the next step's merged reaction
-// draw: its type byte is pending until the next drift kernel resolves it
-// (types are below 16, so the bit never belongs to a type).
-constexpr uint32_t RX_PENDING = 0x80u;
-
 // Slot of the candidate list of a step: three slots, so that a drift kernel
-// can read the slot of its own step, append to the next one and clear the
-// one after (consumed two steps earlier) without racing.
+// appends to the next step's slot and clears the one consumed two steps
+// earlier, never the slot that the kernels around it read.
 __host__ __device__ inline int rx_slot(long long step) {
   return (int)(((step % 3) + 3) % 3);
 }

@@ -109,9 +109,6 @@ struct rdsim_handle {
   bool rx_pre = true;                // reaction prefilter (see rx_may_react)
   int4* rx_list = nullptr;           // [3][npad] prefiltered particles
   int* rx_count = nullptr;           // [3]
-  uint32_t* rtype = nullptr;         // meta after a merged reaction step
-  bool merge_rx = false;             // graph periods resolve listed draws in
-                                     // the drift kernel (no reaction kernel)
   int W = 0;                         // list width (entries per particle)
   int npad = 0;                      // particle stride of the list
   std::vector<Chunk> chunks_h;
@@ -268,7 +265,6 @@ Args make_args(rdsim_handle* h) {
   a.W = h->W;
   a.rx_list = h->rx_list;
   a.rx_count = h->rx_count;
-  a.rtype = h->rtype;
   a.sid = h->sid;
   a.npad = h->npad;
   a.single = h->nsys == 1 ? 1 : 0;
@@ -380,7 +376,6 @@ int force(rdsim_handle* h, long long step, int flags, const double* xi_next, boo
   }
   CK(cudaGetLastError());
   if (flags & F_EM) h->cx = 1 - h->cx;
-  if (flags & F_RX_MERGED) h->cm = 1 - h->cm;  // it wrote this step's types
   return 0;
 }
 
@@ -532,17 +527,10 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
     int rc = rebuild(h, 0, pre, true);
     for (int i = 0; i < h->freq && !rc; i++) {
       // the prefiltered particles of step i are listed by the list builder
-      // (i = 0) or by the drift kernel of step i - 1; with merge_rx the drift
-      // kernel of step i >= 1 resolves them itself
+      // (i = 0) or by the drift kernel of step i - 1
       const bool flagged = pre, flag_next = pre && i + 1 < h->freq;
-      const bool merged = pre && h->merge_rx && i >= 1;
-      const bool merged_next = pre && h->merge_rx && i + 1 < h->freq;
-      if (h->has_rx && !merged) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
-      if (!rc)
-        rc = force(h, i,
-                   F_EM | kf | (flag_next ? F_RX_NEXT : 0) | (merged_next ? F_RX_FLAG : 0) |
-                       (merged ? F_RX_MERGED : 0),
-                   nullptr, true);
+      if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
+      if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
     }
     if (!rc) launch(k_set_counter, 1, 1, h->stream, h->step_dev, h->freq, 1);
     cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
@@ -584,7 +572,7 @@ void free_all(rdsim_handle* h) {
   F(h->sys_d); F(h->laws_d); F(h->walls_d); F(h->rx_d); F(h->tmpl_d);
   F(h->terms_d); F(h->atomterm_d); F(h->cell_count); F(h->cell_start); F(h->bsum);
   F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
-  F(h->chunks_d); F(h->nbr); F(h->ncnt); F(h->rx_list); F(h->rx_count); F(h->rtype);
+  F(h->chunks_d); F(h->nbr); F(h->ncnt); F(h->rx_list); F(h->rx_count);
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); F(h->xp[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
@@ -673,7 +661,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   int total_cells = 0;
   double skin_report = 0, cell_report = 1e300, range_report = 0;
   bool rx_pre_worth = true;  // few draws expected to pass the bound
-  double listed_expect = 0;  // expected prefiltered particles per step
   if (opt.threads_per_particle == 1 || opt.threads_per_particle == 2 ||
       opt.threads_per_particle == 4 || opt.threads_per_particle == 8)
     h->ltpp = opt.threads_per_particle;
@@ -982,9 +969,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       // the prefilter pays when few draws can succeed
       for (int t = 0; t < MAXT; t++)
         if (S.dt * (sd.rxA[t] + sd.rxB[t] * expect) > 0.02) rx_pre_worth = false;
-      double pmax = 0;
-      for (int t = 0; t < MAXT; t++) pmax = std::max(pmax, S.dt * (sd.rxA[t] + sd.rxB[t] * expect));
-      listed_expect += S.n_particles * std::min(1.0, pmax);
     }
     // cells
     int ncs = 1;
@@ -1140,10 +1124,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
   h->ncells = total_cells;
   h->nscan = std::max(1, (total_cells + SCAN_TILE - 1) / SCAN_TILE);
   if (opt.reaction_prefilter < 0 || (opt.reaction_prefilter == 0 && !rx_pre_worth)) h->rx_pre = false;
-  // every CTA of a merged drift kernel scans the step's candidate list: only
-  // for short lists (float32 forces; graph replays only)
-  h->merge_rx = h->rx_pre && h->has_rx && !h->f64 && opt.use_graphs >= 0 &&
-                opt.react_in_drift >= 0 && listed_expect <= 2048.0;
   // list kernels: CTA chunks per system; list width from the expected
   // population (rows beyond it are regenerated from the cells)
   {
@@ -1229,7 +1209,6 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     if ((rc = dalloc(&h->ncnt, N, &B))) return bail(rc);
     if ((rc = dalloc(&h->rx_list, 3 * (size_t)h->npad, &B))) return bail(rc);
     if ((rc = dalloc(&h->rx_count, 3, &B))) return bail(rc);
-    if ((rc = dalloc(&h->rtype, N, &B))) return bail(rc);
     if (cudaMemsetAsync(h->rx_count, 0, 3 * sizeof(int), h->stream) != cudaSuccess)
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
   }
@@ -1755,7 +1734,6 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
   info->device_bytes = h->device_bytes;
   info->reaction_prefilter = (h->rx_pre && h->has_rx) ? 1 : 0;
   info->force_precision = h->f64 ? 1 : 0;
-  info->react_in_drift = h->merge_rx ? 1 : 0;
   return 0;
 }
 

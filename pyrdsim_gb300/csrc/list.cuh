@@ -512,7 +512,7 @@ template <int D, int TPP>
 __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Args& a, int4 rec,
                                      int lane) {
   const int m = rec.x, cnt = rec.z, pid = rec.w;
-  const uint32_t mm = (uint32_t)rec.y & ~RX_PENDING;
+  const uint32_t mm = (uint32_t)rec.y;
   const int tm = mm & 0xff;
   uint32_t cw[4] = {0u, 0u, 0u, 0u};
   if ((s.rx_nb_mask >> tm) & 1) {
@@ -525,7 +525,7 @@ __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Arg
       int d[3];
       const float r2 = pair_geom<D>(s, nb.x, xm, d);
       if (!(r2 < Rrx2)) return;
-      const unsigned int rmask = s.rxmatch[tm * MAXT + (nb.m & 0x7f)];
+      const unsigned int rmask = s.rxmatch[tm * MAXT + (nb.m & 0xff)];
       double dexact = -1.0;
       for (unsigned int b = rmask; b; b &= b - 1u) {
         const int r = __ffs(b) - 1;
@@ -549,78 +549,6 @@ __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Arg
     for (int w = 0; w < 4; w++) cw[w] = __reduce_add_sync(0xffffffffu, cw[w]);
   }
   return lane == 0 ? react_decide<D>(s, rx, a, pid, tm, cw) : tm;
-}
-
-// Global cell index of sorted particle i (its cell at the last rebuild).
-template <int D>
-__device__ inline int global_cell(const SysDev& s, const Args& a, int i) {
-  int g = 0, mult = 1;
-#pragma unroll
-  for (int k = 0; k < D; k++) {
-    g += cell_coord(s, k, a.xr[k][i]) * mult;
-    mult *= s.nc[k];
-  }
-  return s.c0 + g;
-}
-
-// True if a cell of the 3^D stencil around particle m's cell lies in the
-// global cell range [cf, cl].  Lists are built from the same stencils, so a
-// particle of a CTA whose cells span [cf, cl] can have m in its list only
-// if this holds (and m itself lies in that CTA only if it holds).
-template <int D>
-__device__ inline bool stencil_meets(const SysDev& s, const Args& a, int m, int cf, int cl) {
-  int c[3] = {0, 0, 0};
-#pragma unroll
-  for (int k = 0; k < D; k++) c[k] = cell_coord(s, k, a.xr[k][m]);
-  constexpr int NROW = D == 3 ? 9 : (D == 2 ? 3 : 1);
-  const int h1 = D > 1 ? s.halo[1] : 0;
-  const int h2 = D > 2 ? s.halo[2] : 0;
-  bool hit = false;
-#pragma unroll
-  for (int q = 0; q < NROW; q++) {
-    const int dz = D == 3 ? q / 3 - 1 : 0;
-    const int dy = D >= 2 ? q % 3 - 1 : 0;
-    int row, lo0, hi0, lo1, hi1;
-    if (!(dy >= -h1 && dy <= h1 && dz >= -h2 && dz <= h2 &&
-          row_runs<D>(s, c, dy, dz, row, lo0, hi0, lo1, hi1)))
-      continue;
-    const int g0 = s.c0 + row;
-    hit = hit || (g0 + lo0 <= cl && g0 + hi0 >= cf) ||
-          (hi1 >= lo1 && g0 + lo1 <= cl && g0 + hi1 >= cf);
-  }
-  return hit;
-}
-
-// The merged reaction step of a drift kernel (F_RX_MERGED): every listed
-// particle of this step whose stencil meets the CTA's cells is resolved here,
-// a warp per particle, and its new meta word stored in rtype.  Several CTAs
-// may resolve the same particle; they compute and store the same word.  The
-// caller synchronises before reading rtype.
-template <int D, int TPP>
-__device__ __noinline__ void resolve_for_cta(const SysDev& s, const Args& a, const Chunk& ch, int n,
-                                       const int4* list) {
-  const int warp = (int)(threadIdx.x >> 5), l32 = (int)(threadIdx.x & 31);
-  const int cf = global_cell<D>(s, a, ch.beg), cl = global_cell<D>(s, a, ch.beg + ch.cnt - 1);
-  const int4 zero = make_int4(0, 0, 0, 0);
-  for (int b = warp * 32; b < n; b += LBLOCK) {
-    const int q = b + l32;
-    const int4 rec = q < n ? list[q] : zero;
-    const SysDev& sm = a.single ? s : a.sys[a.sid[rec.x]];
-    const bool rel = q < n && stencil_meets<D>(sm, a, rec.x, cf, cl);
-    unsigned int bal = __ballot_sync(0xffffffffu, rel);
-    while (bal) {
-      const int src = __ffs(bal) - 1;
-      bal &= bal - 1u;
-      int4 r;
-      r.x = __shfl_sync(0xffffffffu, rec.x, src);
-      r.y = __shfl_sync(0xffffffffu, rec.y, src);
-      r.z = __shfl_sync(0xffffffffu, rec.z, src);
-      r.w = __shfl_sync(0xffffffffu, rec.w, src);
-      const SysDev& sr = a.single ? s : a.sys[a.sid[r.x]];
-      const int newt = resolve_listed<D, TPP>(sr, a.rx + sr.rx0, a, r, l32);
-      if (l32 == 0) a.rtype[r.x] = (((uint32_t)r.y & ~RX_PENDING) & 0xffffff00u) | (uint32_t)newt;
-    }
-  }
 }
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
@@ -650,17 +578,10 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   for (int k = 0; k < D; k++) xo[k] = a.xp[k][i];
   if (a.stamps && threadIdx.x == 0)
     a.stamps[((size_t)(eff_step(a) % a.stamp_ring) * gridDim.x + blockIdx.x) * 2] = global_timer();
-  uint32_t mi = a.meta[i];
-  const bool merged = (a.flags & F_RX_MERGED) != 0;
-  const int nrx = merged ? a.rx_count[rx_slot(eff_step(a))] : 0;
+  const uint32_t mi = a.meta[i];
   prefetch_rows<TPP>(a, ch, cnt, active);
   __syncthreads();
   const SysDev& s = sh.sys;
-  if (nrx > 0) {  // this step's listed reaction draws (uniform over the CTA)
-    resolve_for_cta<D, TPP>(s, a, ch, nrx, a.rx_list + (size_t)rx_slot(eff_step(a)) * a.npad);
-    __syncthreads();
-    if (mi & RX_PENDING) mi = a.rtype[i];
-  }
   float acc[3] = {0.f, 0.f, 0.f};
   if (active && s.R2 > 0.f) {
     const int ti = mi & 0xff;
@@ -668,8 +589,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
       if (nb.v < 0) return;  // same molecule: reactions only
       int d[3];
       const float r2 = pair_geom<D>(s, nb.x, xo, d);
-      // a neighbour listed for this step's reaction: its new type
-      const int tj = (nb.m & RX_PENDING) ? (int)(a.rtype[nb.v] & 0xff) : (int)(nb.m & 0xff);
+      const int tj = nb.m & 0xff;
       if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
       const unsigned int pp = s.ppair[ti * MAXT + tj];
       const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
@@ -705,8 +625,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     float accb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < D; k++) accb[k] = sacc[k][tid];
-    uint32_t mb = a.meta[ib];
-    if (mb & RX_PENDING) mb = a.rtype[ib];  // resolved above (merged step)
+    const uint32_t mb = a.meta[ib];
     const int pid = a.pid[ib];
     // one Philox call for the next step's noise and reaction uniform
     const bool words = (a.flags & F_RX_NEXT) ||
@@ -715,13 +634,10 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     if (words) w0 = noise_words(s.seed, eff_em_step(a), pid, 0u);
     force_tail<D>(s, sh.walls, a, ib, pid, xb, mb, accb, words ? &w0 : nullptr);
     if (a.flags & F_RX_NEXT) {
+      a.meta_out[ib] = mb;  // the next step's types, unless its draw succeeds
       rec = make_int4(ib, (int)mb, a.ncnt[ib], pid);
       listed = rx_may_react<D>(s, (int)(mb & 0xff), rec.z, pid, eff_em_step(a), &w0);
     }
-    // the next step's types, unless its draw succeeds (then pending when the
-    // next drift kernel resolves it)
-    if (a.flags & (F_RX_NEXT | F_RX_MERGED))
-      a.meta_out[ib] = (listed && (a.flags & F_RX_FLAG)) ? (mb | RX_PENDING) : mb;
   }
   if (a.flags & F_RX_NEXT) {
     // append the particles whose draw may succeed (warp-aggregated)

@@ -107,8 +107,7 @@ class Engine:
     """
 
     def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, use_graphs=True,
-                 list_width=0, reaction_prefilter=None, autotune=False, precision="float32",
-                 react_in_drift=True):
+                 list_width=0, reaction_prefilter=None, autotune=False, precision="float32"):
         """``autotune=True`` picks ``skin`` and ``threads_per_particle`` by
         timing short runs of this batch (:mod:`pyrdsim_gb300.autotune`,
         cached per workload).  ``precision="float64"`` evaluates pair and
@@ -137,7 +136,6 @@ class Engine:
         opt.use_graphs = 0 if use_graphs else -1
         opt.list_width = list_width
         opt.force_precision = 1 if precision == "float64" else 0
-        opt.react_in_drift = 0 if react_in_drift else -1
         # None: automatic; True: whenever the rates allow; False: off
         opt.reaction_prefilter = 0 if reaction_prefilter is None else (1 if reaction_prefilter else -1)
         h = C.c_void_p()
