@@ -11,7 +11,7 @@
 //   pid[buf][i]    i32  particle index in the caller's order
 // Fixed point per dimension k of a system with box length L:
 //   periodic   : X in [0, 2^64) represents X * L / 2^64 (wraps exactly)
-//   reflecting : X in [0, S], S = 2^63 - 2^34, represents X * L / S
+//   reflecting : X in [0, S], S = 2^62, represents X * L / S
 // The pair kernels read only the pair words: (int32)(pj - pi) is the
 // displacement in units of q_k = (length per fixed unit) * 2^ps_k, the
 // minimum image in periodic dimensions (the wrap of X at 2^64 carries over
@@ -19,7 +19,9 @@
 // ps_k is the smallest shift whose range (2^31 q_k) holds twice the largest
 // per-dimension separation of listed pairs, so q_k is about 1e-9 to 1e-8
 // length units whatever the box length.  The squared distance is formed from
-// the exact integer squares d_k^2, each rounded once to float32.  The
+// the exact integer squares d_k^2: summed exactly and rounded once where
+// every dimension has the same unit (square boxes: the reflecting scale is
+// chosen so), each rounded once to float32 otherwise.  The
 // cell-list rebuild uses the high words (bits 32..63).
 #pragma once
 
@@ -99,6 +101,7 @@ struct SysDev {
   int ps[3];                      // pair-word shift
   float qf[3];                    // length per pair-word unit
   float q2[3];                    // its square
+  int qeq;                        // 1: every dimension has the same q_k
   // Bonds: with one fixed unit in every dimension, squared bond lengths are
   // exact 128-bit integers in units of unit^2 (bonded_terms).
   int bond128;                    // 1: every dimension has the same unit

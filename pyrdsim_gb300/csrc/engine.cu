@@ -49,7 +49,11 @@ int fail(int code, const std::string& msg) {
 
 constexpr double TWO32 = 4294967296.0;
 constexpr double TWO64 = 18446744073709551616.0;
-const long long S_REFLECT = (long long)((1ULL << 63) - (1ULL << 34));
+// Reflecting dimensions map [0, L] to [0, 2^62]: positions down to -L (an
+// initial condition may lie below 0) still fit a signed 64-bit word, and the
+// fixed unit L / 2^62 is a power-of-two multiple of a periodic dimension's
+// L / 2^64, so square boxes get equal pair-word units in every dimension.
+const long long S_REFLECT = (long long)(1ULL << 62);
 
 struct HostSys {
   int p0, n, pid0;
@@ -741,6 +745,10 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         sd.unitf[k] = (float)sd.unit_d[k];
         max_q = std::max(max_q, q);
       }
+      sd.qeq = 1;
+      for (int k = 1; k < D; k++)
+        if (sd.qf[k] != sd.qf[0] || std::ldexp(sd.unit_d[k], sd.ps[k]) != std::ldexp(sd.unit_d[0], sd.ps[0]))
+          sd.qeq = 0;
       sd.bond128 = 1;
       for (int k = 1; k < D; k++)
         if (sd.unit_d[k] != sd.unit_d[0]) sd.bond128 = 0;

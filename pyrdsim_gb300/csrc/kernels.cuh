@@ -176,6 +176,12 @@ __device__ inline float lj6_over_r(float c0, float c1, float r2, float w) {
 // integers): each d_k^2 is exact in 64 bits and rounded once to float32.
 template <int D>
 __device__ inline float pair_r2(const SysDev& s, const int* d) {
+  if (s.qeq) {  // one unit: the exact sum of squares, rounded once
+    unsigned long long R = 0ull;
+#pragma unroll
+    for (int k = 0; k < D; k++) R += (unsigned long long)((long long)d[k] * d[k]);
+    return __ull2float_rn(R) * s.q2[0];
+  }
   float r2 = 0.f;
 #pragma unroll
   for (int k = 0; k < D; k++) {

@@ -18,7 +18,7 @@ SRC = r'''
 int main() {
   double x, L;
   int per;
-  const long long Si = (long long)((1ULL << 63) - (1ULL << 34));
+  const long long Si = (long long)(1ULL << 62);
   while (std::scanf("%la %la %d", &x, &L, &per) == 3) {
     unsigned long long X = 0;
     bool ok = rd::fixed_from_double(x, L, per != 0, Si, &X);
@@ -30,7 +30,7 @@ int main() {
 
 
 def exact(x, L, per):
-    Si = 2 ** 63 - 2 ** 34
+    Si = 2 ** 62
     if per:
         f = F(math.fmod(x, L))
         return math.floor(f * 2 ** 64 / F(L) + F(1, 2)) % 2 ** 64

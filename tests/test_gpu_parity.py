@@ -338,7 +338,7 @@ def test_state_upload_is_exact_and_idempotent():
     eng.set_state(x1, t)
     x2, _ = eng.state()
     np.testing.assert_array_equal(x1, x2)
-    unit = np.where(np.asarray(m.periodic) > 0, L / 2.0 ** 64, L / (2.0 ** 63 - 2.0 ** 34))
+    unit = np.where(np.asarray(m.periodic) > 0, L / 2.0 ** 64, L / 2.0 ** 62)
     ref = x.copy()
     ref[1, 0] += L[0]
     # one fixed-point unit, plus the rounding of the float64 read-back
