@@ -18,10 +18,8 @@
 // to the 32-bit difference) and the plain displacement in reflecting ones.
 // ps_k is the smallest shift whose range (2^31 q_k) holds twice the largest
 // per-dimension separation of listed pairs, so q_k is about 1e-9 to 1e-8
-// length units whatever the box length.  The squared distance is formed from
-// the exact integer squares d_k^2: summed exactly and rounded once where
-// every dimension has the same unit (square boxes: the reflecting scale is
-// chosen so), each rounded once to float32 otherwise.  The
+// length units whatever the box length (the high words alone resolve L/2^32).
+// Each difference is rounded once to float32 and scaled by q_k.  The
 // cell-list rebuild uses the high words (bits 32..63).
 #pragma once
 
@@ -100,8 +98,7 @@ struct SysDev {
   float unitf[3];                 // length per fixed unit (float32)
   int ps[3];                      // pair-word shift
   float qf[3];                    // length per pair-word unit
-  float q2[3];                    // its square
-  int qeq;                        // 1: every dimension has the same q_k
+
   // Bonds: with one fixed unit in every dimension, squared bond lengths are
   // exact 128-bit integers in units of unit^2 (bonded_terms).
   int bond128;                    // 1: every dimension has the same unit

@@ -52,7 +52,7 @@ constexpr double TWO64 = 18446744073709551616.0;
 // Reflecting dimensions map [0, L] to [0, 2^62]: positions down to -L (an
 // initial condition may lie below 0) still fit a signed 64-bit word, and the
 // fixed unit L / 2^62 is a power-of-two multiple of a periodic dimension's
-// L / 2^64, so square boxes get equal pair-word units in every dimension.
+// L / 2^64 (square boxes get one pair-word unit in every dimension).
 const long long S_REFLECT = (long long)(1ULL << 62);
 
 struct HostSys {
@@ -741,14 +741,9 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         sd.ps[k] = ps;
         const double q = std::ldexp(sd.unit_d[k], ps);
         sd.qf[k] = (float)q;
-        sd.q2[k] = (float)(q * q);
         sd.unitf[k] = (float)sd.unit_d[k];
         max_q = std::max(max_q, q);
       }
-      sd.qeq = 1;
-      for (int k = 1; k < D; k++)
-        if (sd.qf[k] != sd.qf[0] || std::ldexp(sd.unit_d[k], sd.ps[k]) != std::ldexp(sd.unit_d[0], sd.ps[0]))
-          sd.qeq = 0;
       sd.bond128 = 1;
       for (int k = 1; k < D; k++)
         if (sd.unit_d[k] != sd.unit_d[0]) sd.bond128 = 0;

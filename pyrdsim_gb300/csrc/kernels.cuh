@@ -172,25 +172,6 @@ __device__ inline float lj6_over_r(float c0, float c1, float r2, float w) {
   return fmaf(-eta, cs * fmaf(7.0f, s, -4.0f) * w, g);
 }
 
-// Squared distance of a pair from its pair-word differences d_k (exact
-// integers): each d_k^2 is exact in 64 bits and rounded once to float32.
-template <int D>
-__device__ inline float pair_r2(const SysDev& s, const int* d) {
-  if (s.qeq) {  // one unit: the exact sum of squares, rounded once
-    unsigned long long R = 0ull;
-#pragma unroll
-    for (int k = 0; k < D; k++) R += (unsigned long long)((long long)d[k] * d[k]);
-    return __ull2float_rn(R) * s.q2[0];
-  }
-  float r2 = 0.f;
-#pragma unroll
-  for (int k = 0; k < D; k++) {
-    const long long dk = d[k];
-    r2 = fmaf(__ull2float_rn((unsigned long long)(dk * dk)), s.q2[k], r2);
-  }
-  return r2;
-}
-
 // A 128-bit unsigned integer rounded to the nearest float32: the top 64
 // significant bits, with the bits below them folded into a sticky bit (which
 // lies far below float32's rounding position), converted once.

@@ -287,13 +287,19 @@ __device__ inline Nb gather(const Args& a, int v) {
   return n;
 }
 
-// Pair-word differences of an entry (exact) and its squared distance.
+// Displacement of an entry from its pair words (the exact integer
+// difference rounded once to float32, then scaled by the unit) and the
+// squared distance.
 template <int D>
 __device__ inline float pair_geom(const SysDev& s, const uint32_t* xj, const uint32_t* xi,
-                                  int* d) {
+                                  float* dx) {
+  float r2 = 0.f;
 #pragma unroll
-  for (int k = 0; k < D; k++) d[k] = (int)(xj[k] - xi[k]);
-  return pair_r2<D>(s, d);
+  for (int k = 0; k < D; k++) {
+    dx[k] = (float)(int)(xj[k] - xi[k]) * s.qf[k];
+    r2 = fmaf(dx[k], dx[k], r2);
+  }
+  return r2;
 }
 
 // Visit the list entries of particle i on this lane (entries lane, lane +
@@ -522,7 +528,7 @@ __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Arg
     const float Rrx2 = s.Rrx2;
     auto count = [&](const Nb& nb) {
       const int j = nb.v & 0x7fffffff;
-      int d[3];
+      float d[3];
       const float r2 = pair_geom<D>(s, nb.x, xm, d);
       if (!(r2 < Rrx2)) return;
       const unsigned int rmask = s.rxmatch[tm * MAXT + (nb.m & 0xff)];
@@ -587,7 +593,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
     const int ti = mi & 0xff;
     for_entries<D, TPP>(s, a, i, lane, cnt, [&](const Nb& nb) {
       if (nb.v < 0) return;  // same molecule: reactions only
-      int d[3];
+      float d[3];
       const float r2 = pair_geom<D>(s, nb.x, xo, d);
       const int tj = nb.m & 0xff;
       if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
@@ -602,7 +608,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
         fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
       }
 #pragma unroll
-      for (int k = 0; k < D; k++) acc[k] = fmaf(fr, (float)d[k] * s.qf[k], acc[k]);
+      for (int k = 0; k < D; k++) acc[k] = fmaf(fr, d[k], acc[k]);
     });
   }
 #pragma unroll
@@ -729,7 +735,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_react_l(Args a) 
   if (active && ((s.rx_nb_mask >> ti) & 1)) {
     const float Rrx2 = s.Rrx2;
     for_entries<D, TPP>(s, a, i, lane, cnt, [&](const Nb& nb) {
-      int d[3];
+      float d[3];
       const float r2 = pair_geom<D>(s, nb.x, xo, d);
       if (!(r2 < Rrx2)) return;
       const unsigned int rm = s.rxmatch[ti * MAXT + (nb.m & 0xff)];
