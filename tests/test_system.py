@@ -160,3 +160,82 @@ def test_simulate_saves_and_appends_trajectory():
         files = os.listdir(d)
         assert any(f.startswith("trajectory.h5") for f in files)
     assert np.isfinite(res2["x"]).all()
+
+
+def _trajectory_file(d):
+    """Frames, types and step count of the saved trajectory in directory d
+    (HDF5 when h5py is installed, else the NumPy archive beside it)."""
+    try:
+        import h5py
+        with h5py.File(os.path.join(d, "trajectory.h5"), "r") as hf:
+            return (np.asarray(hf["trajectory"][()]), np.asarray(hf["trajectory_types"][()]),
+                    int(hf["N_steps_completed"][()]))
+    except ImportError:
+        with np.load(os.path.join(d, "trajectory.h5.npz")) as z:
+            return z["trajectory"], z["trajectory_types"], int(z["N_steps_completed"])
+
+
+def _run_decks(texts, steps_list, seed):
+    """simulate() once per entry of steps_list (N_steps), the first from the
+    initial condition and the others with append=True; returns the last
+    result and the saved trajectory file."""
+    from pyrdsim_gb300 import system
+    with in_deck(texts) as d:
+        res = None
+        for k, n in enumerate(steps_list):
+            t = dict(texts)
+            t["parameters"] = t["parameters"].replace("N_steps = 40", f"N_steps = {n}")
+            with open(os.path.join(d, "parameters.txt"), "w") as f:
+                f.write(t["parameters"])
+            s = system({"seed": seed})
+            res = s.simulate(verbose=False, append=k > 0)
+        return res, _trajectory_file(d)
+
+
+@pytest.mark.gpu
+def test_resumed_run_continues_the_same_trajectory():
+    """A 40-step run saved at step 20 and appended with the same seed
+    reproduces the continuous 40-step run (pyrdsim.pyx:1703-1786, 2429-2444):
+    the counter-based noise is keyed by (seed, step, particle), so the
+    resumed run draws the same numbers.  Types and the saved frames' types
+    are identical; positions agree to 1e-9 (the save stores float64
+    positions, one rounding of the 64-bit fixed point)."""
+    fx = load_fixture("two_species_wall_rx")
+    texts = deck_dict(fx)
+    texts["parameters"] = texts["parameters"].replace("N_out = 100000", "N_out = 20")
+    cont, (fc, tc, nc) = _run_decks(texts, [40], seed=4)
+    split, (fs, ts, ns) = _run_decks(texts, [20, 40], seed=4)
+    assert nc == ns == 40
+    assert fc.shape == fs.shape and fc.shape[0] == 3  # step 20, then frames 30 and 40
+    np.testing.assert_array_equal(split["particle_types"], cont["particle_types"])
+    np.testing.assert_array_equal(ts, tc)
+    L = np.array([18.2, 12.0])
+
+    def close(a, b):
+        d = a - b
+        d[..., 0] -= L[0] * np.round(d[..., 0] / L[0])
+        return np.abs(d).max() <= 1e-9 * max(1.0, np.abs(b).max())
+    assert close(split["x"], cont["x"])
+    assert close(fs, fc)
+    # and a different seed gives a different continuation
+    other, _ = _run_decks(texts, [20, 40], seed=5)
+    assert not close(other["x"], cont["x"])
+
+
+@pytest.mark.gpu
+def test_trajectory_file_in_hdf5():
+    """With h5py installed the trajectory goes to HDF5 with the reference's
+    datasets (pyrdsim.pyx:1725-1786)."""
+    h5py = pytest.importorskip("h5py")
+    fx = load_fixture("two_species_wall_rx")
+    texts = deck_dict(fx)
+    texts["parameters"] = texts["parameters"].replace("N_out = 100000", "N_out = 20")
+    from pyrdsim_gb300 import system
+    with in_deck(texts) as d:
+        system({"seed": 4}).simulate(verbose=False)
+        with h5py.File(os.path.join(d, "trajectory.h5"), "r") as hf:
+            assert set(hf.keys()) >= {"trajectory", "trajectory_types", "molecule_ids",
+                                      "first_index_of_molecule", "N_steps_completed",
+                                      "N_particles", "N_molecules", "dt_trajectory",
+                                      "N_species", "stride", "L"}
+            assert hf["trajectory"].shape[0] == 3 and int(hf["N_steps_completed"][()]) == 40
