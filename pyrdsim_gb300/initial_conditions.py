@@ -10,15 +10,22 @@ the one whose first atom lies farthest from the first atoms already placed
 whole system with a full ``simulate()`` run after every insertion.
 
 Here the placement rule is the same, with the nearest-first-atom distances
-from a k-d tree of the placed first atoms (rebuilt every 64
-insertions, the newest ones compared directly), and the relaxation runs once
-for the finished system on the GPU engine (``simulate`` with its noise),
-followed by the reference's check that no two listed partners of different
-molecules are closer than ``min_distance_threshold_sim``.  Reference
-configurations without files come from minimising the reference's bonded
-energy from ten random starts with scipy's derivative-free Powell method
-(the reference uses CMA-ES from the ``cma`` package).  Random numbers come
-from a seeded numpy generator (the reference's are unseeded).
+from a k-d tree of the placed first atoms (rebuilt every 64 insertions, the
+newest ones compared directly).  The relaxation follows the reference's
+loop: from the fourth molecule on, the system placed so far is relaxed with
+a full ``simulate()`` run on the GPU engine, and the insertion is rejected
+and retried (at most 1000 times) when that run raises RuntimeError or
+ZeroDivisionError, when two listed partners of different molecules end up
+closer than ``min_distance_threshold_sim``, or when a position is not
+finite; an accepted run's positions replace the placed ones.  The only
+difference: ``relax_every`` > 1 relaxes after every relax_every insertions
+instead of after each one (a rejection then removes and redraws the whole
+batch), which keeps large systems affordable; 1 is the reference's
+behaviour.  Reference configurations without files come from minimising the
+reference's bonded energy from ten random starts with scipy's
+derivative-free Powell method (the reference uses CMA-ES from the ``cma``
+package).  Random numbers come from a seeded numpy generator (the
+reference's are unseeded).
 """
 from __future__ import annotations
 
@@ -147,10 +154,13 @@ class _Nearest:
 
 
 def generate(N_particles, particle_types, n_atoms, references, L, n_dim, rng,
-             min_distance_threshold):
-    """Molecule placement (pyrdsim.pyx:2720-2826 without the relaxation runs).
-    Returns the reference's output array: molecule number, index in molecule,
-    molecule id, particle type, positions."""
+             min_distance_threshold, relax=None, relax_every=1):
+    """Molecule placement and relaxation (pyrdsim.pyx:2720-2826).  ``relax``
+    (optional) takes the output array of the molecules placed so far and
+    returns their relaxed positions, or None to reject (see the module
+    docstring); it runs after molecule 4, 4 + relax_every, ... and after the
+    last one.  Returns the reference's output array: molecule number, index
+    in molecule, molecule id, particle type, positions."""
     order = np.zeros(0, dtype=int)
     total = 0
     for mid, n in N_particles.items():
@@ -160,7 +170,11 @@ def generate(N_particles, particle_types, n_atoms, references, L, n_dim, rng,
     out = np.zeros((total, n_dim + 4))
     near = _Nearest(n_dim)
     count = 0
-    for i, e in enumerate(order):
+    # the last relaxed (accepted) state: molecules placed, particles
+    kept_i, kept_count, rejected = 0, 0, 0
+    i = 0
+    while i < len(order):
+        e = order[i]
         conf = references[e]
         for _ in range(N_TRIES):
             if i > 0:
@@ -183,4 +197,22 @@ def generate(N_particles, particle_types, n_atoms, references, L, n_dim, rng,
             out[count, 4:] = f
             count += 1
         near.add(placed[0])
+        i += 1
+        due = i > 3 and ((i - 3) % max(1, int(relax_every)) == 0 or i == len(order))
+        if relax is None or not due:
+            continue
+        relaxed = relax(out[:count].copy())
+        if relaxed is not None:
+            out[:count, 4:] = relaxed
+            kept_i, kept_count, rejected = i, count, 0
+            continue
+        rejected += 1
+        if rejected >= N_TRIES:
+            raise RuntimeError("Could not place molecule {0}".format(i))
+        # remove the rejected insertions and draw them again
+        i, count = kept_i, kept_count
+        out[count:] = 0.0
+        near = _Nearest(n_dim)
+        for m in np.flatnonzero(out[:count, 1] == 0):
+            near.add(out[m, 4:])
     return out

@@ -241,15 +241,20 @@ class system:  # noqa: N801  (the reference's class name)
     def create_initial_conditions(self, N_particles, particle_types,
                                   reference_configurations=None,
                                   min_distance_threshold=None,
-                                  min_distance_threshold_sim=None, relax=True):
+                                  min_distance_threshold_sim=None, relax=True,
+                                  relax_every=1):
         """pyrdsim.pyx:2634-2828: place N_particles[molecule_id] molecules of
         each type (atom types particle_types[molecule_id]) at random, each at
         the best of 1000 random poses for the distance of its first atom to
-        the first atoms already placed, write the initial-condition file and
-        relax the system with ``simulate`` (see
-        :mod:`pyrdsim_gb300.initial_conditions` for what differs from the
-        reference).  Returns the array (molecule number, index in molecule,
-        molecule id, particle type, positions)."""
+        the first atoms already placed; from the fourth molecule on relax the
+        system with ``simulate`` after every insertion (every
+        ``relax_every`` insertions), rejecting and redrawing the insertion
+        when the run fails (RuntimeError, ZeroDivisionError), leaves listed
+        partners of different molecules closer than
+        ``min_distance_threshold_sim`` or a non-finite position.  Writes the
+        initial-condition file; returns the array (molecule number, index in
+        molecule, molecule id, particle type, positions).  ``relax_log``
+        records (molecules, accepted, min distance) of every relaxation."""
         from . import initial_conditions as ic
         m = self._model
         if min_distance_threshold is None:
@@ -271,20 +276,27 @@ class system:  # noqa: N801  (the reference's class name)
                                         " has {1} atoms, but interaction parameters for that"
                                         " molecule demand {2} atoms").format(
                                             i, len(refs[i]), n_atoms[i]))
+        self.relax_log = []
+
+        def run_relaxation(arr):  # pyrdsim.pyx:2786-2814
+            self._set_state_from_array(arr)
+            self.write_current_state_to_text_file(filename=m.initial_conditions_filename)
+            n_mol = len(self.first_index_of_molecule)
+            try:
+                result = self.simulate(verbose=False, random_force=True)
+            except (RuntimeError, ZeroDivisionError):
+                self.relax_log.append((n_mol, False, float("nan")))
+                return None
+            min_dist = self._engine.observables()["min_distance"]
+            ok = min_dist >= min_distance_threshold_sim and np.isfinite(result["x"]).all()
+            self.relax_log.append((n_mol, bool(ok), float(min_dist)))
+            return result["x"] if ok else None
+
         out = ic.generate(N_particles, particle_types, n_atoms, refs, m.L, D, rng,
-                          min_distance_threshold)
+                          min_distance_threshold, relax=run_relaxation if relax else None,
+                          relax_every=relax_every)
         self._set_state_from_array(out)
         self.write_current_state_to_text_file(filename=m.initial_conditions_filename)
-        if relax and len(self.first_index_of_molecule) > 3:
-            result = self.simulate(verbose=False, random_force=True)
-            relaxed = result["x"]
-            min_dist = self._engine.observables()["min_distance"]
-            if np.isnan(relaxed).any() or min_dist < min_distance_threshold_sim:
-                raise RuntimeError("Min distance {0} below threshold {1} after relaxation".format(
-                    min_dist, min_distance_threshold_sim))
-            out[:, 4:] = relaxed
-            self._set_state_from_array(out)
-            self.write_current_state_to_text_file(filename=m.initial_conditions_filename)
         return out
 
     def _set_state_from_array(self, out):

@@ -79,15 +79,46 @@ def test_reference_configuration_files(tmp_path):
 
 
 @pytest.mark.gpu
-def test_relaxed_initial_conditions_on_the_gpu():
+@pytest.mark.parametrize("relax_every", [1, 4])
+def test_relaxed_initial_conditions_on_the_gpu(relax_every):
+    """The reference's loop (pyrdsim.pyx:2738-2826): from the fourth molecule
+    on every insertion (every batch of relax_every) is relaxed with
+    simulate() and accepted only when the run succeeds with listed partners
+    of different molecules at least min_distance_threshold_sim apart and all
+    positions finite; the final state passes the same checks."""
     fx = load_fixture("patchy")
     with in_deck(deck_dict(fx)):
         s = _patchy_system()
         m = s._model
-        out = s.create_initial_conditions({0: 12}, {0: [0, 1, 1, 2]})
+        out = s.create_initial_conditions({0: 12}, {0: [0, 1, 1, 2]}, relax_every=relax_every)
+        log = s.relax_log
+        accepted = [row for row in log if row[1]]
+        assert [row[0] for row in accepted] == [i for i in range(4, 13)
+                                                if (i - 3) % relax_every == 0 or i == 12]
+        assert all(row[2] >= m.rs / 10 for row in accepted)
+        assert all(not row[1] for row in log if row not in accepted)
         assert np.isfinite(out[:, 4:]).all()
         assert s._engine.observables()["min_distance"] >= m.rs / 10
         assert os.path.exists(m.initial_conditions_filename)
+
+
+def test_rejected_insertions_are_redrawn():
+    """A relaxation that fails removes the insertion(s) since the last
+    accepted state, which are then placed again."""
+    from pyrdsim_gb300 import initial_conditions as ic
+    rng = np.random.default_rng(3)
+    ref = {0: np.array([[0.0, 0.0], [0.5, 0.0]])}
+    calls = []
+
+    def relax(arr):
+        calls.append(len(np.flatnonzero(arr[:, 1] == 0)))
+        return None if len(calls) in (2, 3) else arr[:, 4:] + 0.0
+
+    out = ic.generate({0: 8}, {0: [0, 1]}, {0: 2}, ref, np.array([30.0, 30.0]), 2, rng, 0.5,
+                      relax=relax, relax_every=2)
+    # batches end at 5, 7, 8 molecules; the second call (7) fails twice
+    assert calls == [5, 7, 7, 7, 8]
+    assert np.flatnonzero(out[:, 1] == 0).size == 8 and np.isfinite(out).all()
 
 
 @pytest.mark.parametrize("n_dim", [2, 3])
