@@ -173,6 +173,30 @@ def cpu_baseline(workload, n_gpu_state=None):
     }
 
 
+def _port_worker(a):
+    from oracle import ref_bench
+    workload, n, steps, seed = a
+    return ref_bench.run_sample("port", workload, n, steps, seed)
+
+
+def cpu_baseline_port_all_cores(n=65536, steps=5):
+    """Secondary CPU baseline: the float64 C++ restatement of the step (cell
+    lists, O(N)) at the full N, one independent replica per host core
+    (spawned processes), throughput summed over the replicas."""
+    import multiprocessing as mp
+    procs = max(1, os.cpu_count() or 1)
+    with mp.get_context("spawn").Pool(procs) as pool:
+        pool.map(_port_worker, [("active_wall_fluid", 4096, 1, p) for p in range(procs)])
+        t0 = time.perf_counter()
+        secs = pool.map(_port_worker, [("active_wall_fluid", n, steps, 50 + p)
+                                       for p in range(procs)])
+        wall = time.perf_counter() - t0
+    return {"value": procs * n * steps / max(secs), "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"float64 C++ restatement (cell lists), active wall fluid at N={n} "
+                      f"(tanh wall), {procs} replicas x {steps} steps each, one per core, "
+                      f"slowest replica {max(secs):.2f} s (wall {wall:.2f} s)"}
+
+
 def fp64_drift(sd, x, types, device):
     """Plain PyTorch float64 drift of one system at positions x: the pair laws
     (pyrdsim.pyx:1068-1130) over every pair of different molecules within
@@ -622,6 +646,10 @@ def run_ours(args, rank, ws, local):
             out["cpu_baseline"] = cpu_baseline("active_wall_fluid")
         except Exception as exc:
             out["cpu_baseline"] = {"unavailable": str(exc)[:200]}
+        try:
+            out["cpu_baseline_all_cores"] = cpu_baseline_port_all_cores()
+        except Exception as exc:
+            out["cpu_baseline_all_cores"] = {"unavailable": str(exc)[:200]}
         try:
             out["force_err_vs_fp64"] = force_error(eng, sd, f"cuda:{local}")
         except Exception as exc:
