@@ -231,7 +231,8 @@ __device__ inline void em_update_d(const SysDev& s, const Args& a, int sysi, int
     const double dl = fp * acc[k] + np * xi[k];
     const double v = dl * s.inv_unit_d[k];
     long long d = 0;
-    if (!(fabs(v) < 4.0e18)) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, dl, em_step);
+    // the bound of delta_fixed: |d| < 2^61 (advance() needs |d| < 2^62)
+    if (!(fabs(v) < 2.3e18)) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, dl, em_step);
     else d = __double2ll_rn(v);
     advance(s, a, gi, pid, k, d, em_step);
   }

@@ -283,7 +283,9 @@ struct WordLoad {
 
 __device__ inline long long delta_fixed(float d, float inv_unit_hi, bool* bad) {
   float v = d * inv_unit_hi;
-  if (!(fabsf(v) < 1073741824.0f)) {  // non-finite or > a quarter box
+  // non-finite, or beyond 2^29 high units (an eighth of a periodic box, half
+  // a reflecting one): |result| < 2^62, which advance() relies on
+  if (!(fabsf(v) < 536870912.0f)) {
     *bad = true;
     return 0;
   }
@@ -349,10 +351,11 @@ __device__ inline void gaussians(const U4& w, float* xi) {
   }
 }
 
-// Advances coordinate k of particle gi by d fixed units and applies the
-// boundary condition (pyrdsim.pyx:2253-2292): an exact wrap in periodic
-// dimensions, a reflection at 0 and L in 128-bit arithmetic in reflecting
-// ones (2 S overflows int64).  Writes the high, low and pair words.
+// Advances coordinate k of particle gi by d fixed units (|d| < 2^62) and
+// applies the boundary condition (pyrdsim.pyx:2253-2292): an exact wrap in
+// periodic dimensions, a reflection at 0 and L in reflecting ones, where X
+// lies in [-S, S] (S = 2^62), so X + d and the reflections stay within
+// int64.  Writes the high, low and pair words.
 __device__ inline void advance(const SysDev& s, const Args& a, int gi, int pid, int k,
                                long long d, long long em_step) {
   unsigned long long X = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
@@ -360,9 +363,9 @@ __device__ inline void advance(const SysDev& s, const Args& a, int gi, int pid, 
     X += (unsigned long long)d;
   } else {
     // reflect (pyrdsim.pyx:2275-2280)
-    __int128 Xs = (__int128)(long long)X + d;
-    const __int128 Si = s.Si[k];
-    if (Xs > Si) Xs = 2 * Si - Xs;
+    long long Xs = (long long)X + d;
+    const long long Si = s.Si[k];
+    if (Xs > Si) Xs = Si - (Xs - Si);
     if (Xs < 0) Xs = -Xs;
     if (Xs < 0 || Xs > Si) {
       record_error(a.err, RDSIM_ERR_OUT_OF_BOUNDS, pid, k,
