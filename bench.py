@@ -578,7 +578,8 @@ def run_ours(args, rank, ws, local):
     barrier(ws)
     clk = clocks.stop() if clocks else None
     timed = eng.profile()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    seg_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(seg_ms)
     ms_max = max_over_ranks(ms, ws)
     value = ws * N * seg * args.steps / (ms_max / 1e3)
     launches = sum(v["launches"] for k, v in timed.items() if k not in ("hook", "drift_span"))
@@ -635,6 +636,7 @@ def run_ours(args, rank, ws, local):
                                "CTA end minus first CTA start, averaged over the launches",
                      "peak_source": peak_kind,
                      "drift_share_of_timed": span["ms"] / ms},
+        "segment_us_per_step": [round(1e3 * m / seg, 3) for m in seg_ms],
         "kernel_launches": {k: v["launches"] for k, v in timed.items() if k != "drift_span"},
         "serialised_kernel_us": {k: 1e3 * v["ms"] / max(1, v["timed"])
                                  for k, v in ser.items() if k != "drift_span" and v["timed"]},
