@@ -328,12 +328,15 @@ int rebuild(rdsim_handle* h, long long step = 0, bool prefilter = false, bool re
   const int n = h->N;
   ProfScope ps(h, P_REBUILD, h->ncells <= SCAN1_T * SCAN1_I ? 5 : 6);
   uint32_t* const* x = h->xh[h->cx];
+  // a captured period advances the step counter by one period in k_bin
+  long long* ctr = rel ? h->step_dev : nullptr;
+  const long long add = h->freq;
   if (h->D == 2)
-    launch(k_bin<2>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+    launch(k_bin<2>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count, ctr, add);
   else if (h->D == 3)
-    launch(k_bin<3>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+    launch(k_bin<3>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count, ctr, add);
   else
-    launch(k_bin<1>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count);
+    launch(k_bin<1>, nblk(n), 256, h->stream, h->sys_d, h->sid, x[0], x[1], x[2], n, h->cell_of, h->rank_of, h->cell_count, ctr, add);
   if (h->ncells <= SCAN1_T * SCAN1_I) {
     launch(k_scan_one, 1, SCAN1_T, h->stream, h->cell_count, h->ncells, h->cell_start);
   } else {
@@ -518,7 +521,8 @@ bool snapshot_in(rdsim_handle* h, long long a, long long b) {
 // One rebuild period (steps s .. s+freq-1, each ending with the fused EM
 // update of the next step) as a CUDA graph.  Graphs are cached per buffer
 // parity state; kernel step numbers are offsets from a device counter that
-// the graph advances by freq at its end.
+// the graph's first kernel (k_bin) advances by freq: before a replay of the
+// period starting at s it holds s - freq.
 int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
   const int key = h->cx | (h->cm << 1) | (h->co << 2) | ((kf & F_NO_NOISE) ? 8 : 0);
   auto it = h->graph_cache.find(key);
@@ -536,7 +540,6 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
       if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
       if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
     }
-    if (!rc) launch(k_set_counter, 1, 1, h->stream, h->step_dev, h->freq, 1);
     cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
     if (rc) {
       if (g) cudaGraphDestroy(g);
@@ -556,10 +559,11 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
     h->cm = cm0;
     h->co = co0;
   }
-  if (h->step_dev_value != s) launch(k_set_counter, 1, 1, h->stream, h->step_dev, s, 0);
+  if (h->step_dev_value != s - h->freq)
+    launch(k_set_counter, 1, 1, h->stream, h->step_dev, s - h->freq, 0);
   CK(cudaGetLastError());
   CK(cudaGraphLaunch(it->second.exec, h->stream));
-  h->step_dev_value = s + h->freq;
+  h->step_dev_value = s;
   for (int c = 0; c < RDSIM_PROFILE_CLASSES; c++) h->nlaunch[c] += it->second.launches[c];
   const int flips = (1 + h->freq) & 1;  // rebuild + freq updates / reactions
   h->cx ^= flips;

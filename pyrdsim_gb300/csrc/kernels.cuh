@@ -740,11 +740,15 @@ __global__ void k_em(Args a, const int* sid) {
 
 // ---------------------------------------------------------------------------
 // Cell-list rebuild.
+// ctr (graph replays): the device step counter, advanced here by `add` at
+// the start of a rebuild period (the kernels that read it run after this one).
 template <int D>
 __global__ void k_bin(const SysDev* sysv, const int* sid, const uint32_t* x0, const uint32_t* x1,
-                      const uint32_t* x2, int n, int* cell_of, int* rank_of, int* count) {
+                      const uint32_t* x2, int n, int* cell_of, int* rank_of, int* count,
+                      long long* ctr, long long add) {
   pdl_trigger();
   pdl_wait();
+  if (ctr && blockIdx.x == 0 && threadIdx.x == 0) *ctr += add;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool valid = i < n;
