@@ -660,12 +660,11 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   // the slot of two steps ago was consumed before this kernel: empty it for
   // the drift kernel (or list builder) of the next step that appends to it
   if (blockIdx.x == 0 && threadIdx.x == 0) a.rx_count[rx_slot(eff_step(a) + 2)] = 0;
-  if (a.stamps) {
-    __syncthreads();
-    if (threadIdx.x == 0)
-      a.stamps[((size_t)(eff_step(a) % a.stamp_ring) * gridDim.x + blockIdx.x) * 2 + 1] =
-          global_timer();
-  }
+  // each warp's end: the CTA's end is their maximum (no barrier; the times
+  // only grow, so a reused slot's older value never wins)
+  if (a.stamps && (threadIdx.x & 31) == 0)
+    atomicMax(a.stamps + ((size_t)(eff_step(a) % a.stamp_ring) * gridDim.x + blockIdx.x) * 2 + 1,
+              global_timer());
 }
 
 // Spans of the stamped drift launches: per ring slot, the last CTA end minus
