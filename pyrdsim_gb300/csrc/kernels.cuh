@@ -536,6 +536,11 @@ __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const A
       const float e = expf(-2.0f * fabsf(z));
       f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
     } else {
+      // the high word alone first (it is at most the coordinate): all but
+      // the particles near the wall stop here without reading the low word
+      const float yh = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) *
+                       s.unit_hi[W.dim];
+      if (yh > W.rc_hi) continue;
       // the full coordinate; reflecting ones are signed (an initial
       // position may lie below 0)
       const unsigned long long X = ((unsigned long long)h << 32) | a.xl[W.dim][gi];
@@ -627,7 +632,7 @@ __device__ inline double rx_total(const SysDev& s, const RxDev* rx, int ti, cons
 // total propensity).
 template <int D>
 __device__ inline int react_decide(const SysDev& s, const RxDev* rx, const Args& a, int pid,
-                                   int ti, const uint32_t* cw) {
+                                   int ti, const uint32_t* cw, const U4* w0 = nullptr) {
   int newt = ti;
   const bool any = (s.rx_any_mask >> ti) & 1;
   if (any) {  // pyrdsim.pyx:2211-2222
@@ -640,7 +645,7 @@ __device__ inline int react_decide(const SysDev& s, const RxDev* rx, const Args&
       u1lo = __double2float_rd(a.u1[pid]);
       u1hi = __double2float_ru(a.u1[pid]);
     } else {
-      u1_words<D>(s.seed, step, pid, nullptr, h1, l1);
+      u1_words<D>(s.seed, step, pid, w0, h1, l1);
       uniform_bounds(h1, u1lo, u1hi);
     }
     const bool screen = (s.rx_screen_mask >> ti) & 1;

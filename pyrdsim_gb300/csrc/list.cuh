@@ -518,6 +518,10 @@ template <int D, int TPP>
 __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Args& a, int4 rec,
                                      int lane) {
   const int m = rec.x, cnt = rec.z, pid = rec.w;
+  // lane 0's counter-based words of the draw (2D: u1 from the tag-0 words),
+  // computed while the neighbour loads below are in flight
+  U4 w0 = {0u, 0u, 0u, 0u};
+  if (D <= 2 && lane == 0 && !(a.flags & F_INJECT)) w0 = noise_words(s.seed, eff_step(a), pid, 0u);
   const uint32_t mm = (uint32_t)rec.y;
   const int tm = mm & 0xff;
   uint32_t cw[4] = {0u, 0u, 0u, 0u};
@@ -554,7 +558,9 @@ __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Arg
 #pragma unroll
     for (int w = 0; w < 4; w++) cw[w] = __reduce_add_sync(0xffffffffu, cw[w]);
   }
-  return lane == 0 ? react_decide<D>(s, rx, a, pid, tm, cw) : tm;
+  return lane == 0 ? react_decide<D>(s, rx, a, pid, tm, cw,
+                                     (D <= 2 && !(a.flags & F_INJECT)) ? &w0 : nullptr)
+                   : tm;
 }
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
