@@ -1,7 +1,7 @@
 """The float64 -> 64-bit fixed-point conversion of state uploads
 (fixed_from_double in csrc/kernels.cuh) is exact: compiled for the host and
 checked against rational arithmetic (periodic: round(frac(x/L) 2^64) with
-halves up, mod 2^64; reflecting: llround(x/L S), S = 2^63 - 2^34)."""
+halves up, mod 2^64; reflecting: llround(x/L S), S = 2^62)."""
 import math
 import os
 import shutil
