@@ -144,18 +144,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def traffic_per_launch(n):
-    """dram bytes per k_force_l launch from the committed ncu summary (scaled
-    by particles if the capture was a smaller case), or None."""
-    path = os.path.join(ROOT, "profiles", "k_force_l_active_wall_fluid.md")
+def traffic_per_launch(n, steps=1, period=False):
+    """dram bytes per launch of the dominant kernel (k_period: ``steps``
+    integration steps per launch; k_force_l: one) from the committed ncu
+    summary, per particle and step, or None."""
+    name = "k_period_active_wall_fluid.md" if period else "k_force_l_active_wall_fluid.md"
+    key = "traffic_bytes_per_particle_step:" if period else "traffic_bytes_per_particle:"
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_particle:"):
-                    return float(line.split(":")[1]) * n
+                if line.startswith(key):
+                    return float(line.split(":")[1]) * n * steps
     except Exception:
         pass
     return None
+
+
+def dominant_kernel(eng, sd):
+    """(kernel name, integration steps per launch) of the drift work: the
+    period kernel runs a whole rebuild period per launch."""
+    if eng.info()["period_kernel"]:
+        return "k_period<2,2>", sd.model.neighbor_list_update_frequency
+    return "k_force_l<2,2>", 1
 
 
 def cpu_baseline(workload, n_gpu_state=None):
@@ -497,11 +507,13 @@ def n_sweep(local, sizes=((65536, 1000), (1048576, 200), (4194304, 100))):
         ms = _events_ms([eng.stream()], lambda: eng.step(steps))
         prof = eng.profile()
         span = prof["drift_span"]
+        kname, per = dominant_kernel(eng, sd)
         us = 1e3 * span["ms"] / max(1, span["launches"])
-        ach = ALG_BYTES * n / (us / 1e6) / 1e9
+        ach = ALG_BYTES * n * per / (us / 1e6) / 1e9
         rows.append({"n_particles": n, "steps": steps,
                      "particle_steps_per_s": n * steps / (ms / 1e3),
-                     "us_per_step": 1e3 * ms / steps,
+                     "us_per_step": 1e3 * ms / steps, "kernel": kname,
+                     "steps_per_launch": per,
                      "drift_span_us": us, "drift_achieved_gbs": ach,
                      "drift_frac_of_measured_hbm": ach / peak,
                      "device_bytes": eng.info()["device_bytes"]})
@@ -586,8 +598,9 @@ def run_ours(args, rank, ws, local):
     span = timed["drift_span"]
     span_us = 1e3 * span["ms"] / max(1, span["launches"])
     peak, peak_kind = peaks()
-    achieved = ALG_BYTES * N / (span_us / 1e6) / 1e9
-    traffic = traffic_per_launch(N)
+    kname, per = dominant_kernel(eng, sd)
+    achieved = ALG_BYTES * N * per / (span_us / 1e6) / 1e9
+    traffic = traffic_per_launch(N, per, per > 1)
     # a short serialised pass (CUDA events around every launch; no graphs)
     # for the per-class split; not the timed pass
     eng.set_profiling(True, stamps=False)
@@ -629,8 +642,9 @@ def run_ours(args, rank, ws, local):
                 "path": "C ABI: rdsim_set_state (host) + rdsim_step + rdsim_get_state (host)"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "kernel": "k_force_l<2,2>",
-                     "algorithmic_bytes_per_launch": ALG_BYTES * N,
+                     "frac": achieved / peak, "traffic": traffic, "kernel": kname,
+                     "integration_steps_per_launch": per,
+                     "algorithmic_bytes_per_launch": ALG_BYTES * N * per,
                      "avg_launch_us": span_us, "launches_timed": span["launches"],
                      "timing": "device global-timer stamps in the timed graph replays: last "
                                "CTA end minus first CTA start, averaged over the launches",

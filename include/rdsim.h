@@ -48,7 +48,10 @@ enum {
   RDSIM_ERR_SKIN = 18,        /* a particle moved more than half the skin
                                  (Euclidean; dim = -1) between two rebuilds */
   RDSIM_ERR_NONFINITE = 19,   /* non-finite or larger-than-box displacement  */
-  RDSIM_ERR_CAPACITY = 20     /* a per-call buffer was too small             */
+  RDSIM_ERR_CAPACITY = 20,    /* a per-call buffer was too small             */
+  RDSIM_ERR_SYNC = 21         /* a wait of the period kernel on the progress
+                                 of neighbouring chunks ran out (no GPU hang:
+                                 every CTA gives up and returns)           */
 };
 
 /* ---- model description (parsed decks) ---------------------------------- */
@@ -156,7 +159,14 @@ typedef struct {
                                      may succeed (same results).  0: when few
                                      draws are expected to pass the bound;
                                      > 0: whenever the rates allow; < 0: off  */
-  int32_t reserved[5];
+  int32_t period_kernel;          /* >= 0: graph-replayed rebuild periods run
+                                     as one launch of the period kernel when
+                                     every chunk of particles fits on the GPU
+                                     at once (same results); < 0: one drift
+                                     and one reaction launch per step        */
+  int32_t sync_wait_ms;           /* limit of one wait of the period kernel on
+                                     its neighbouring chunks; <= 0: 1000 ms   */
+  int32_t reserved[3];
 } rdsim_options;
 
 /* rdsim_step flags */
@@ -306,6 +316,9 @@ typedef struct {
   int64_t device_bytes;
   int32_t reaction_prefilter;     /* 1: on for this handle                    */
   int32_t force_precision;        /* as in rdsim_options                      */
+  int32_t period_kernel;          /* 1: rebuild periods replay as one launch of
+                                     the period kernel                       */
+  int32_t pad;
 } rdsim_info;
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 
@@ -331,6 +344,12 @@ typedef struct {
 int rdsim_set_profiling(rdsim_handle* h, int32_t enable);
 /* Fills *p and resets the counters (synchronises the stream). */
 int rdsim_get_profile(rdsim_handle* h, rdsim_profile* p);
+
+/* Test hook, no counterpart in the reference: chunk `chunk` (a CTA of the
+ * period kernel) stops publishing its progress, so that the waits of its
+ * neighbours run out after sync_wait_ms and the next rdsim_step returns
+ * RDSIM_ERR_SYNC.  -1 restores normal operation. */
+int rdsim_test_withhold(rdsim_handle* h, int32_t chunk);
 
 /* Message of the last failing call on this thread. */
 const char* rdsim_last_error(void);

@@ -22,6 +22,7 @@ ERR_ANGLE_DOMAIN = 17
 ERR_SKIN = 18
 ERR_NONFINITE = 19
 ERR_CAPACITY = 20
+ERR_SYNC = 21
 
 LAW_LJ = 1
 LAW_TANH = 2
@@ -109,7 +110,8 @@ class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("skin", C.c_double),
                 ("threads_per_particle", C.c_int32), ("force_precision", C.c_int32),
                 ("use_graphs", C.c_int32), ("list_width", C.c_int32),
-                ("reaction_prefilter", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("reaction_prefilter", C.c_int32), ("period_kernel", C.c_int32),
+                ("sync_wait_ms", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class Info(C.Structure):
@@ -118,7 +120,8 @@ class Info(C.Structure):
                 ("list_width", C.c_int32), ("skin", C.c_double),
                 ("cell_size_min", C.c_double), ("interaction_range", C.c_double),
                 ("device_bytes", C.c_int64), ("reaction_prefilter", C.c_int32),
-                ("force_precision", C.c_int32)]
+                ("force_precision", C.c_int32), ("period_kernel", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 RDF_OTHER_MOLECULES = 1

@@ -201,6 +201,43 @@ struct Args {
   // values of each CTA's start and end, slot = step mod ring
   unsigned long long* stamps;
   int stamp_ring;
+  // period kernel (list.cuh: k_period), written by the list builder with
+  // F_PERIOD_PREP: per chunk, the bitmap of the chunks its particles read
+  // (list entries and bonded partners, itself included; PMASK_WORDS words),
+  // the particles whose reaction draw of the rebuild step may succeed
+  // (CAND_WORDS words, bit = particle within the chunk) and the progress word
+  uint32_t* nbmask;
+  uint32_t* cand0;
+  int* pflag;
+  long long wait_ns;              // period kernel: limit of one wait (ns)
+};
+
+// Period kernel: a particle whose reaction draw of the next step is pending
+// carries this bit in that step's type word (bits 21-23 of the atom-index
+// byte are otherwise zero: at most 32 atoms per molecule) until its chunk
+// has resolved the draw and written the final word.
+constexpr uint32_t META_PENDING = 1u << 23;
+
+// Period kernel limits: chunks of one launch (bitmap width) and particles
+// per chunk (candidate mask width).
+constexpr int PMASK_WORDS = 40;
+constexpr int PMAX_CHUNKS = PMASK_WORDS * 32;
+constexpr int CAND_WORDS = 4;
+// Ints per progress word of the period kernel (32: one 128-byte line each,
+// so that the ~20 CTAs polling a chunk do not share a line with others).
+#ifndef RD_PERIOD_FLAG_STRIDE
+#define RD_PERIOD_FLAG_STRIDE 32
+#endif
+constexpr int PFLAG_STRIDE = RD_PERIOD_FLAG_STRIDE;
+
+// Arguments of the period kernel besides its four step-argument blocks.
+struct PeriodArgs {
+  int nsteps;                     // steps of the rebuild period
+  int nchunks;                    // chunks = CTAs (all resident)
+  int rx;                         // prefiltered reaction phases run
+  int withhold;                   // test hook: this chunk never publishes
+                                  // its progress (-1: none)
+  long long wait_ns;              // limit of one wait (global timer, ns)
 };
 
 __device__ inline unsigned long long global_timer() {
@@ -219,7 +256,12 @@ enum : int {
   F_RX_NEXT = 64,                 // drift kernel: copy the types forward and
                                   // list the particles whose reaction draw of
                                   // the next step may succeed
-  F_RX_HERE = 128                 // list builder: the same for its own step
+  F_RX_HERE = 128,                // list builder: the same for its own step
+  F_PERIOD = 256,                 // step kernels inside k_period: the step
+                                  // number is the CTA's current step
+  F_PERIOD_PREP = 512             // list builder: write the period kernel's
+                                  // neighbour-chunk bitmaps, progress words
+                                  // and (with F_RX_HERE) candidate masks
 };
 
 // Slot of the candidate list of a step: three slots, so that a drift kernel

@@ -115,6 +115,13 @@ struct rdsim_handle {
   int* rx_count = nullptr;           // [3]
   int W = 0;                         // list width (entries per particle)
   int npad = 0;                      // particle stride of the list
+  // period kernel (list.cuh: k_period): one launch per graph-replayed period
+  bool period_on = false;
+  uint32_t* nbmask = nullptr;        // [chunks][PMASK_WORDS]
+  uint32_t* cand0 = nullptr;         // [chunks][CAND_WORDS]
+  int* pflag = nullptr;              // [chunks] progress words
+  int withhold = -1;                 // test hook (rdsim_test_withhold)
+  long long wait_ns = 1000000000LL;
   std::vector<Chunk> chunks_h;
   Chunk* chunks_d = nullptr;
   int* nbr = nullptr;
@@ -277,6 +284,9 @@ Args make_args(rdsim_handle* h) {
     a.stamp_ring = h->stamp_ring;
   }
   if (!h->chunks_h.empty()) a.chunk1 = h->chunks_h[0];
+  a.nbmask = h->nbmask;
+  a.cand0 = h->cand0;
+  a.pflag = h->pflag;
   return a;
 }
 
@@ -324,7 +334,8 @@ unsigned nblk(int n, int b = 256) { return (unsigned)((n + b - 1) / b); }
 // `prefilter`: the list builder also runs the reaction prefilter of `step`
 // (then the reaction kernel of that step visits the listed particles only);
 // `rel`: step numbers are offsets from the device counter (graph capture).
-int rebuild(rdsim_handle* h, long long step = 0, bool prefilter = false, bool rel = false) {
+int rebuild(rdsim_handle* h, long long step = 0, bool prefilter = false, bool rel = false,
+            bool period_prep = false) {
   const int n = h->N;
   ProfScope ps(h, P_REBUILD, h->ncells <= SCAN1_T * SCAN1_I ? 5 : 6);
   uint32_t* const* x = h->xh[h->cx];
@@ -360,7 +371,7 @@ int rebuild(rdsim_handle* h, long long step = 0, bool prefilter = false, bool re
   Args b = make_args(h);
   b.step = step;
   b.step_base = rel ? h->step_dev : nullptr;
-  b.flags = prefilter ? F_RX_HERE : 0;
+  b.flags = (prefilter ? F_RX_HERE : 0) | (period_prep ? F_PERIOD_PREP : 0);
   if (h->D == 2) launch_nlist<2>(h, b);
   else if (h->D == 3) launch_nlist<3>(h, b);
   else launch_nlist<1>(h, b);
@@ -444,6 +455,11 @@ int check_device_error(rdsim_handle* h) {
   CK(cudaStreamSynchronize(h->stream));
   if (e.code == 0) return 0;
   CK(cudaMemsetAsync(h->err, 0, sizeof(ErrDev), h->stream));
+  if (h->period_on) {
+    // a period kernel that stopped early may leave draws marked pending
+    k_clear_pending<<<nblk(h->N), 256, 0, h->stream>>>(h->meta[0], h->meta[1], h->N);
+    CK(cudaGetLastError());
+  }
   char buf[256];
   if (e.code == RDSIM_ERR_OUT_OF_BOUNDS) {
     snprintf(buf, sizeof buf,
@@ -458,6 +474,11 @@ int check_device_error(rdsim_handle* h) {
     snprintf(buf, sizeof buf,
              "non-finite or larger-than-box update of particle %lld, dimension %d "
              "(value %.6g) at step %lld", e.particle, e.dim, e.value, e.step);
+  } else if (e.code == RDSIM_ERR_SYNC) {
+    snprintf(buf, sizeof buf,
+             "period kernel: chunk %lld waited longer than the limit for the progress of "
+             "its neighbouring chunks (step %lld); the state of this call is not valid",
+             e.particle, e.step);
   } else {
     snprintf(buf, sizeof buf, "device error %d at step %lld", e.code, e.step);
   }
@@ -518,6 +539,83 @@ bool snapshot_in(rdsim_handle* h, long long a, long long b) {
   return first <= b;
 }
 
+template <int D>
+void launch_period_d(rdsim_handle* h, const Args* A, const PeriodArgs& p) {
+  const dim3 g((unsigned)p.nchunks);
+  if (h->ltpp == 1) launch(k_period<D, 1>, g, LBLOCK, h->stream, A[0], A[1], A[2], A[3], p);
+  else if (h->ltpp == 2) launch(k_period<D, 2>, g, LBLOCK, h->stream, A[0], A[1], A[2], A[3], p);
+  else if (h->ltpp == 8) launch(k_period<D, 8>, g, LBLOCK, h->stream, A[0], A[1], A[2], A[3], p);
+  else launch(k_period<D, 4>, g, LBLOCK, h->stream, A[0], A[1], A[2], A[3], p);
+}
+
+// The steps of one rebuild period after its rebuild (which ran with
+// period_prep) as one launch of the period kernel: the drift arguments of
+// steps of parity P read positions xh[cx ^ P] and the types after the
+// step's reactions; the reaction arguments read the types before them.
+// Step numbers are offsets from the device counter.
+int period_launch(rdsim_handle* h, int kf, bool pre) {
+  const int cx0 = h->cx, cm0 = h->cm;
+  Args A[4];
+  for (int P = 0; P < 2; P++) {
+    h->cx = cx0 ^ P;
+    h->cm = cm0 ^ P;
+    Args r = make_args(h);
+    h->cm = h->has_rx ? (cm0 ^ P ^ 1) : cm0;
+    Args d = make_args(h);
+    d.flags = F_EM | F_CHECK_SKIN | F_PERIOD | kf;
+    r.flags = F_PERIOD | kf;
+    d.step_base = r.step_base = h->step_dev;
+    d.step = r.step = 0;
+    d.wait_ns = r.wait_ns = h->wait_ns;
+    A[P] = d;
+    A[2 + P] = r;
+  }
+  h->cx = cx0;
+  h->cm = cm0;
+  PeriodArgs p;
+  std::memset(&p, 0, sizeof p);
+  p.nsteps = h->freq;
+  p.nchunks = (int)h->chunks_h.size();
+  p.rx = pre ? 1 : 0;
+  p.withhold = h->withhold;
+  p.wait_ns = h->wait_ns;
+  {
+    ProfScope ps(h, P_FORCE, 1);
+    if (h->D == 2) launch_period_d<2>(h, A, p);
+    else if (h->D == 3) launch_period_d<3>(h, A, p);
+    else launch_period_d<1>(h, A, p);
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// Resident CTAs of the period kernel on the handle's device (0 if unknown).
+template <int D>
+int period_capacity_d(int tpp) {
+  int nb = 0;
+  cudaError_t e;
+  if (tpp == 1) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_period<D, 1>, LBLOCK, 0);
+  else if (tpp == 2) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_period<D, 2>, LBLOCK, 0);
+  else if (tpp == 8) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_period<D, 8>, LBLOCK, 0);
+  else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_period<D, 4>, LBLOCK, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return nb;
+}
+
+int period_capacity(rdsim_handle* h) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int nb = h->D == 2 ? period_capacity_d<2>(h->ltpp)
+                           : (h->D == 3 ? period_capacity_d<3>(h->ltpp) : period_capacity_d<1>(h->ltpp));
+  return nb * sms;
+}
+
 // One rebuild period (steps s .. s+freq-1, each ending with the fused EM
 // update of the next step) as a CUDA graph.  Graphs are cached per buffer
 // parity state; kernel step numbers are offsets from a device counter that
@@ -532,13 +630,18 @@ int run_period_graph(rdsim_handle* h, long long s, int kf, bool pre) {
     std::memcpy(before, h->nlaunch, sizeof before);
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = rebuild(h, 0, pre, true);
-    for (int i = 0; i < h->freq && !rc; i++) {
-      // the prefiltered particles of step i are listed by the list builder
-      // (i = 0) or by the drift kernel of step i - 1
-      const bool flagged = pre, flag_next = pre && i + 1 < h->freq;
-      if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
-      if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
+    const bool one_launch = h->period_on && (pre || !h->has_rx);
+    int rc = rebuild(h, 0, pre, true, one_launch);
+    if (one_launch) {
+      if (!rc) rc = period_launch(h, kf, pre);
+    } else {
+      for (int i = 0; i < h->freq && !rc; i++) {
+        // the prefiltered particles of step i are listed by the list builder
+        // (i = 0) or by the drift kernel of step i - 1
+        const bool flagged = pre, flag_next = pre && i + 1 < h->freq;
+        if (h->has_rx) rc = react(h, i, kf, nullptr, nullptr, true, flagged);
+        if (!rc) rc = force(h, i, F_EM | kf | (flag_next ? F_RX_NEXT : 0), nullptr, true);
+      }
     }
     cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
     if (rc) {
@@ -581,6 +684,7 @@ void free_all(rdsim_handle* h) {
   F(h->terms_d); F(h->atomterm_d); F(h->cell_count); F(h->cell_start); F(h->bsum);
   F(h->cell_of); F(h->rank_of); F(h->tmp); F(h->sid); F(h->slot_of);
   F(h->chunks_d); F(h->nbr); F(h->ncnt); F(h->rx_list); F(h->rx_count);
+  F(h->nbmask); F(h->cand0); F(h->pflag);
   for (int b = 0; b < 2; b++) {
     for (int k = 0; k < 3; k++) { F(h->xh[b][k]); F(h->xl[b][k]); F(h->xp[b][k]); }
     F(h->meta[b]); F(h->mol[b]); F(h->pid[b]);
@@ -1220,6 +1324,18 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
       return bail(fail(RDSIM_ERR_CUDA, "memset"));
   }
   h->graphs = opt.use_graphs >= 0;
+  // period kernel: float32 forces, every chunk resident at once (its CTAs
+  // wait for each other) and within the neighbour-chunk bitmap
+  if (opt.sync_wait_ms > 0) h->wait_ns = (long long)opt.sync_wait_ms * 1000000LL;
+  {
+    const int nch = (int)h->chunks_h.size();
+    if (opt.period_kernel >= 0 && !h->f64 && nch <= PMAX_CHUNKS && nch <= period_capacity(h)) {
+      if ((rc = dalloc(&h->nbmask, (size_t)nch * PMASK_WORDS, &B))) return bail(rc);
+      if ((rc = dalloc(&h->cand0, (size_t)nch * CAND_WORDS, &B))) return bail(rc);
+      if ((rc = dalloc(&h->pflag, (size_t)nch * PFLAG_STRIDE, &B))) return bail(rc);
+      h->period_on = true;
+    }
+  }
   if ((rc = dalloc(&h->cl_d, (size_t)3 * h->nsys, &B))) return bail(rc);
   auto up = [&](void* d, const void* s, size_t bytes) -> int {
     if (bytes == 0) return 0;
@@ -1741,6 +1857,18 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
   info->device_bytes = h->device_bytes;
   info->reaction_prefilter = (h->rx_pre && h->has_rx) ? 1 : 0;
   info->force_precision = h->f64 ? 1 : 0;
+  info->period_kernel = h->period_on ? 1 : 0;
+  return 0;
+}
+
+int rdsim_test_withhold(rdsim_handle* h, int32_t chunk) {
+  if (!h) return fail(RDSIM_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  h->withhold = chunk;
+  // periods are captured with the hook's value: recapture
+  for (auto& g : h->graph_cache) cudaGraphExecDestroy(g.second.exec);
+  h->graph_cache.clear();
   return 0;
 }
 

@@ -34,10 +34,16 @@ __device__ inline void record_error(ErrDev* e, int code, long long particle, int
 __device__ inline void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ inline void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// The step the CTA of a period kernel is at (F_PERIOD): its drift of step n
+// performs the update of step n + 1.
+static __shared__ long long period_step;
+
 __device__ inline long long eff_step(const Args& a) {
+  if (a.flags & F_PERIOD) return period_step;
   return a.step_base ? *a.step_base + a.step : a.step;
 }
 __device__ inline long long eff_em_step(const Args& a) {
+  if (a.flags & F_PERIOD) return period_step + 1;
   return a.step_base ? *a.step_base + a.em_step : a.em_step;
 }
 

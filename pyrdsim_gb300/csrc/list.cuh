@@ -276,7 +276,24 @@ struct Nb {
   int v;  // entry: sorted index | LIST_SAME_MOL
 };
 
-template <int D>
+// The final type word of sorted particle j whose reaction draw is still
+// pending (period kernel): polled until its chunk writes it, for at most
+// a.wait_ns; then RDSIM_ERR_SYNC is recorded and the old word is used.
+__device__ inline uint32_t wait_final_meta(const Args& a, int j, uint32_t v) {
+  const unsigned long long t0 = global_timer();
+  while (v & META_PENDING) {
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(a.meta + j) : "memory");
+    if ((long long)(global_timer() - t0) > a.wait_ns) {
+      record_error(a.err, RDSIM_ERR_SYNC, (long long)j, -2, 0.0, eff_step(a));
+      return v & ~META_PENDING;
+    }
+  }
+  return v;
+}
+
+// PEND (period kernel): a neighbour whose draw of this step is pending is
+// waited for, so that its type is the one after this step's reactions.
+template <int D, bool PEND = false>
 __device__ inline Nb gather(const Args& a, int v) {
   Nb n;
   const int j = v & 0x7fffffff;
@@ -284,6 +301,7 @@ __device__ inline Nb gather(const Args& a, int v) {
 #pragma unroll
   for (int k = 0; k < 3; k++) n.x[k] = k < D ? a.xp[k][j] : 0u;
   n.m = a.meta[j];
+  if (PEND && (n.m & META_PENDING)) n.m = wait_final_meta(a, j, n.m);
   return n;
 }
 
@@ -306,7 +324,7 @@ __device__ inline float pair_geom(const SysDev& s, const uint32_t* xj, const uin
 // TPP, ...), from the list or, for an overflowing row, from the cells.  List
 // rows are read RD_LIST_BATCH entries at a time: all index loads, then all
 // neighbour loads, then the arithmetic.
-template <int D, int TPP, class Fn>
+template <int D, int TPP, bool PEND = false, class Fn>
 __device__ inline void for_entries(const SysDev& s, const Args& a, int i, int lane, int cnt,
                                    Fn&& fn) {
   constexpr int B = RD_LIST_BATCH;
@@ -320,13 +338,13 @@ __device__ inline void for_entries(const SysDev& s, const Args& a, int i, int la
       }
       Nb nb[B];
 #pragma unroll
-      for (int u = 0; u < B; u++) nb[u] = gather<D>(a, v[u]);
+      for (int u = 0; u < B; u++) nb[u] = gather<D, PEND>(a, v[u]);
 #pragma unroll
       for (int u = 0; u < B; u++)
         if (e0 + u * TPP < cnt) fn(nb[u]);
     }
   } else {
-    row_scan<D, TPP>(s, a, i, lane, [&](int, int v) { fn(gather<D>(a, v)); });
+    row_scan<D, TPP>(s, a, i, lane, [&](int, int v) { fn(gather<D, PEND>(a, v)); });
   }
 }
 
@@ -361,7 +379,12 @@ __device__ inline bool rx_may_react(const SysDev& s, int ti, int cnt, int pid, l
 // order (the order row_scan uses), so the row does not depend on NT.  A
 // thread whose rows hold more than BCAP listed pairs rescans them to write
 // the rest.  With F_RX_HERE the first thread of each particle also runs the
-// reaction prefilter of its step with the fresh entry count.
+// reaction prefilter of its step with the fresh entry count.  With
+// F_PERIOD_PREP (CTA = chunk of the period kernel) it also writes the
+// chunk's neighbour-chunk bitmap (the chunks of every list entry, of the
+// bonded partners and the chunk itself), its candidate mask of the rebuild
+// step (instead of the candidate list; their type words carry META_PENDING)
+// and its progress word (0).
 template <int D, int TPP>
 __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Args a) {
   constexpr int PER = LBLOCK / TPP;
@@ -375,6 +398,8 @@ __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Arg
   __shared__ SysDev sys;
   __shared__ int sbuf[NTH][BCAP];
   __shared__ int scnt[NTH];
+  __shared__ uint32_t sbits[PMASK_WORDS];
+  __shared__ uint32_t scand[CAND_WORDS];
   pdl_trigger();
   const Chunk ch = chunk_at<PER>(a, (int)blockIdx.x);
   {
@@ -382,6 +407,11 @@ __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Arg
     WordLoad<NS, NTH> ls;
     ls.load(reinterpret_cast<const int*>(&a.sys[ch.sys]), NS);
     ls.store(reinterpret_cast<int*>(&sys), NS);
+  }
+  const bool prep = (a.flags & F_PERIOD_PREP) != 0;
+  if (prep) {
+    for (int w = (int)threadIdx.x; w < PMASK_WORDS; w += NTH) sbits[w] = 0u;
+    for (int w = (int)threadIdx.x; w < CAND_WORDS; w += NTH) scand[w] = 0u;
   }
   pdl_wait();
   __syncthreads();
@@ -462,9 +492,29 @@ __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Arg
     }
     return k;
   };
+  // period kernel: the chunk of sorted particle j of this system (a
+  // system's chunks are consecutive runs of PER particles) into the bitmap;
+  // runs of entries fall into one chunk, so only changes are marked
+  const int chunk0 = (int)blockIdx.x - (ch.beg - s.p0) / PER;
+  int lastc = -1;
+  auto mark = [&](int j) {
+    const int c = chunk0 + (j - s.p0) / PER;
+    if (c != lastc) {
+      atomicOr(&sbits[c >> 5], 1u << (c & 31));
+      lastc = c;
+    }
+  };
   const int cnt = scan_rows([&](int k, int ent) {
     if (k < BCAP) sbuf[tid][k] = ent;
+    if (prep) mark(ent & 0x7fffffff);
   });
+  if (prep && valid) {
+    mark(i);
+    if (t == 0 && tmi != 0xff) {  // bonded partners: every atom of the molecule
+      const int mb = a.pid[i] - loci, na = a.tmpl[tmi].n_atoms;
+      for (int b = 0; b < na; b++) mark(a.slot_of[mb + b]);
+    }
+  }
   scnt[tid] = cnt;
   __syncthreads();
   int off = 0, total = 0;
@@ -489,13 +539,21 @@ __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Arg
     if (t == 0) {
       a.ncnt_out[i] = total;
       if (a.flags & F_RX_HERE) {  // reaction prefilter of this step (see rx_may_react)
-        a.meta_out[i] = mi;
         rec = make_int4(i, (int)mi, total, a.pid[i]);
         listed = rx_may_react<D>(s, (int)(mi & 0xff), total, rec.w, eff_step(a), nullptr);
+        a.meta_out[i] = mi | ((prep && listed) ? META_PENDING : 0u);
       }
     }
   }
-  if (a.flags & F_RX_HERE) {
+  if (prep) {
+    if (listed) atomicOr(&scand[pp >> 5], 1u << (pp & 31));
+    __syncthreads();
+    const int c = (int)blockIdx.x;
+    for (int w = (int)threadIdx.x; w < PMASK_WORDS; w += NTH)
+      a.nbmask[(size_t)c * PMASK_WORDS + w] = sbits[w];
+    for (int w = (int)threadIdx.x; w < CAND_WORDS; w += NTH) a.cand0[c * CAND_WORDS + w] = scand[w];
+    if (threadIdx.x == 0) a.pflag[c * PFLAG_STRIDE] = 0;
+  } else if (a.flags & F_RX_HERE) {
     const unsigned int bal = __ballot_sync(0xffffffffu, listed);
     if (bal) {
       const int l32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
@@ -563,6 +621,35 @@ __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Arg
                    : tm;
 }
 
+// Phase A of the drift kernels: this lane's share of the pair drift of
+// sorted particle i (type word mi, pair words xo) over its list entries
+// (pyrdsim.pyx:1988-2030), added to acc.
+template <int D, int TPP, bool PEND = false>
+__device__ __forceinline__ void pair_drift(const ListShared& sh, const Args& a, int i, int lane,
+                                           int cnt, const uint32_t* xo, uint32_t mi, float* acc) {
+  const SysDev& s = sh.sys;
+  const int ti = mi & 0xff;
+  for_entries<D, TPP, PEND>(s, a, i, lane, cnt, [&](const Nb& nb) {
+    if (nb.v < 0) return;  // same molecule: reactions only
+    float d[3];
+    const float r2 = pair_geom<D>(s, nb.x, xo, d);
+    const int tj = nb.m & 0xff;
+    if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
+    const unsigned int pp = s.ppair[ti * MAXT + tj];
+    const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
+    float fr;
+    if ((pp & 0x8000u) && r2 < L0.rc2_lo) {
+      // a single Lennard-Jones n = 6 law, clear of its cutoff: eval_pair's
+      // arithmetic inline
+      fr = lj6_over_r(L0.c0, L0.c1, r2, recip(r2));
+    } else {
+      fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
+    }
+#pragma unroll
+    for (int k = 0; k < D; k++) acc[k] = fmaf(fr, d[k], acc[k]);
+  });
+}
+
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
 // list entries (pyrdsim.pyx:1988-2030).  Phase B: one thread per particle
 // adds walls and bonded terms and performs the fused Euler-Maruyama update.
@@ -595,28 +682,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_LIST_MIN_BLOCKS) k_force_l(Args a) 
   __syncthreads();
   const SysDev& s = sh.sys;
   float acc[3] = {0.f, 0.f, 0.f};
-  if (active && s.R2 > 0.f) {
-    const int ti = mi & 0xff;
-    for_entries<D, TPP>(s, a, i, lane, cnt, [&](const Nb& nb) {
-      if (nb.v < 0) return;  // same molecule: reactions only
-      float d[3];
-      const float r2 = pair_geom<D>(s, nb.x, xo, d);
-      const int tj = nb.m & 0xff;
-      if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
-      const unsigned int pp = s.ppair[ti * MAXT + tj];
-      const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
-      float fr;
-      if ((pp & 0x8000u) && r2 < L0.rc2_lo) {
-        // a single Lennard-Jones n = 6 law, clear of its cutoff: eval_pair's
-        // arithmetic inline
-        fr = lj6_over_r(L0.c0, L0.c1, r2, recip(r2));
-      } else {
-        fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
-      }
-#pragma unroll
-      for (int k = 0; k < D; k++) acc[k] = fmaf(fr, d[k], acc[k]);
-    });
-  }
+  if (active && s.R2 > 0.f) pair_drift<D, TPP>(sh, a, i, lane, cnt, xo, mi, acc);
 #pragma unroll
   for (int o = TPP >> 1; o > 0; o >>= 1) {
 #pragma unroll
@@ -835,6 +901,281 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
     const int newt = resolve_listed<D, TPP>(s, rx, a, rec, lane);
     if (lane == 0) a.meta_out[rec.x] = ((uint32_t)rec.y & 0xffffff00u) | (uint32_t)newt;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Period kernel: every step of one rebuild period (the listed reactions of
+// each step, then its drift with the fused update of the next step) in one
+// launch, one CTA per chunk, all CTAs resident.  There is no grid-wide
+// barrier: after its drift of step n a chunk publishes progress n + 1, and
+// a chunk starts step n once every chunk it reads (its list entries' and
+// bonded partners' chunks, from the list builder's bitmap) has progress
+// >= n: their positions of step n and their types are written.  The list
+// relation is symmetric (the same distance and partner tests from both
+// ends), so the chunks that read a chunk are among those it waits for,
+// which also protects the buffers it overwrites.
+// Reactions: the drift of step n - 1 marks the type word of each particle
+// whose draw of step n may succeed with META_PENDING; the particle's own
+// chunk resolves the draw at the start of step n and writes the final word.
+// A neighbour that gathers a pending word waits for that word alone, so
+// only the particles next to a pending draw wait for it (and the symmetric
+// list again orders the resolution's reads of the old types before the
+// neighbour overwrites them).  Every wait ends after wait_ns of the global
+// timer, or as soon as any CTA has recorded an error: RDSIM_ERR_SYNC is
+// recorded and the CTA returns.  The arithmetic per particle is that of
+// k_force_l and k_react_listed (same functions), so the results equal
+// theirs bit for bit.
+
+// Polling: relaxed loads (an acquire load invalidates the SM's L1, which
+// the other CTAs on the SM use for their list rows), then one acquire fence
+// once every word has reached its target.
+#ifndef RD_PERIOD_POLL_ACQUIRE
+#define RD_PERIOD_POLL_ACQUIRE 0
+#endif
+#ifndef RD_PERIOD_SLEEP_NS
+#define RD_PERIOD_SLEEP_NS 32
+#endif
+
+__device__ inline int ld_poll(const int* p) {
+  int v;
+#if RD_PERIOD_POLL_ACQUIRE
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+#else
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+#endif
+  return v;
+}
+
+__device__ inline void fence_acquire() {
+#if !RD_PERIOD_POLL_ACQUIRE
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+#endif
+}
+
+__device__ inline void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+struct PeriodShared {
+  ListShared sh;
+  unsigned short wl[PMAX_CHUNKS];   // chunks waited for (not itself)
+  uint32_t cmask[2][CAND_WORDS];    // listed particles of steps of parity 0/1
+  long long s0;                     // first step of the period
+  int nwl;
+  int ok;
+};
+
+// All threads: true once every listed chunk has published progress >=
+// target; false (after recording the error) if the wait gave up.
+__device__ inline bool period_wait(PeriodShared& ps, const int* pflag, int target,
+                                   const PeriodArgs& p, ErrDev* err, long long step) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    bool ok = true;
+    unsigned long long t0 = 0ull;
+    for (int b = 0; b < ps.nwl && ok; b += 32) {
+      const int c = b + lane < ps.nwl ? (int)ps.wl[b + lane] : -1;
+      for (;;) {
+        const int v = c >= 0 ? ld_poll(pflag + c * PFLAG_STRIDE) : target;
+        if (__all_sync(0xffffffffu, v - target >= 0)) break;
+        bool give_up = false;
+        if (lane == 0) {
+          const unsigned long long now = global_timer();
+          if (t0 == 0ull) t0 = now;
+          const int e = *(volatile int*)&err->code;
+          give_up = e != 0 || (long long)(now - t0) > p.wait_ns;
+          if (give_up && e == 0)
+            record_error(err, RDSIM_ERR_SYNC, (long long)blockIdx.x, -1, (double)target, step);
+        }
+        if (__shfl_sync(0xffffffffu, give_up, 0)) {
+          ok = false;
+          break;
+        }
+        if (RD_PERIOD_SLEEP_NS > 0) __nanosleep(RD_PERIOD_SLEEP_NS);
+      }
+    }
+    fence_acquire();
+    if (lane == 0) ps.ok = ok;
+  }
+  __syncthreads();
+  return ps.ok != 0;
+}
+
+// Publishes progress v of the CTA's chunk; the caller has synchronised the
+// CTA after its last write of the phase.
+__device__ inline void period_publish(int* pflag, int v, const PeriodArgs& p) {
+  if (threadIdx.x == 0 && (int)blockIdx.x != p.withhold) {
+    __threadfence();
+    st_release(pflag + (size_t)blockIdx.x * PFLAG_STRIDE, v);
+  }
+}
+
+// The reaction draw of listed particle m by the calling warp (out of line:
+// rare, and its registers stay out of the drift's budget).
+template <int D, int TPP>
+__device__ __noinline__ void period_resolve(const ListShared& sh, const Args& r, int m, int lane) {
+  const int4 rec = make_int4(m, (int)r.meta[m], r.ncnt[m], r.pid[m]);
+  const int newt = resolve_listed<D, TPP>(sh.sys, sh.rx, r, rec, lane);
+  if (lane == 0) r.meta_out[m] = ((uint32_t)rec.y & 0xffffff00u) | (uint32_t)newt;
+}
+
+// Step n of the period on the CTA's chunk: d / r are the step arguments of
+// the drift and of the reactions (buffers of parity P = n & 1).
+template <int D, int TPP, int P>
+__device__ __forceinline__ bool period_run_step(PeriodShared& ps, float (*sacc)[LBLOCK / TPP],
+                                                const Args& d, const Args& r,
+                                                const PeriodArgs& p, const Chunk& ch, int n) {
+  const int tid = threadIdx.x, warp = tid >> 5, l32 = tid & 31;
+  const SysDev& s = ps.sh.sys;
+  if (tid == 0) period_step = ps.s0 + n;
+  if (!period_wait(ps, d.pflag, n, p, d.err, ps.s0 + n)) return false;
+  // reactions of step n: the chunk's listed particles, a warp each
+  // (k_react_listed's resolution); their neighbours wait for the words
+  if (p.rx) {
+    uint32_t pend = 0u;
+#pragma unroll
+    for (int w = 0; w < CAND_WORDS; w++) pend |= ps.cmask[P][w];
+    if (pend) {
+      int k = 0;
+#pragma unroll 1
+      for (int w = 0; w < CAND_WORDS; w++) {
+        for (uint32_t b = ps.cmask[P][w]; b; b &= b - 1u, k++) {
+          if ((k & (LBLOCK / 32 - 1)) != warp) continue;
+          period_resolve<D, TPP>(ps.sh, r, ch.beg + w * 32 + __ffs(b) - 1, l32);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // drift of step n and the update of step n + 1 (k_force_l)
+  const int g = tid / TPP, lane = tid % TPP;
+  const bool active = g < ch.cnt;
+  const int i = ch.beg + (active ? g : 0);
+  if (tid < ch.cnt) {
+    const int ib = ch.beg + tid;
+    prefetch_l1(d.pid + ib);
+#pragma unroll
+    for (int k = 0; k < D; k++) prefetch_l1(d.xl[k] + ib);
+  }
+  const int cnt = d.ncnt[i];
+  uint32_t xo[3] = {0u, 0u, 0u};
+#pragma unroll
+  for (int k = 0; k < D; k++) xo[k] = d.xp[k][i];
+  const uint32_t mi = d.meta[i];
+  prefetch_rows<TPP>(d, ch, cnt, active);
+  float acc[3] = {0.f, 0.f, 0.f};
+  if (active && s.R2 > 0.f) pair_drift<D, TPP, true>(ps.sh, d, i, lane, cnt, xo, mi, acc);
+#pragma unroll
+  for (int o = TPP >> 1; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < D; k++) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+  }
+  if (active && lane == 0) {
+#pragma unroll
+    for (int k = 0; k < D; k++) sacc[k][g] = acc[k];
+  }
+  __syncthreads();
+  const bool rx_next = p.rx && n + 1 < p.nsteps;
+  const int ib = ch.beg + tid;
+  bool listed = false;
+  if (tid < ch.cnt) {
+    uint32_t xb[3] = {0u, 0u, 0u};
+#pragma unroll
+    for (int k = 0; k < D; k++) xb[k] = d.xh[k][ib];
+    float accb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < D; k++) accb[k] = sacc[k][tid];
+    const uint32_t mb = d.meta[ib];
+    const int pid = d.pid[ib];
+    const bool words = rx_next || !(d.flags & F_NO_NOISE);
+    U4 w0 = {0u, 0u, 0u, 0u};
+    if (words) w0 = noise_words(s.seed, ps.s0 + n + 1, pid, 0u);
+    force_tail<D>(s, ps.sh.walls, d, ib, pid, xb, mb, accb, words ? &w0 : nullptr);
+    if (rx_next) {
+      listed = rx_may_react<D>(s, (int)(mb & 0xff), d.ncnt[ib], pid, ps.s0 + n + 1, &w0);
+      // the next step's type word, marked while its draw is pending
+      d.meta_out[ib] = mb | (listed ? META_PENDING : 0u);
+    }
+  }
+  // the particles whose draw of step n + 1 may succeed: one word per warp
+  const unsigned int bal = __ballot_sync(0xffffffffu, listed);
+  if (l32 == 0 && warp < CAND_WORDS) ps.cmask[P ^ 1][warp] = rx_next ? bal : 0u;
+  __syncthreads();
+  period_publish(d.pflag, n + 1, p);
+  return true;
+}
+
+// Clears the pending marks that a period kernel stopped by an error leaves.
+static __global__ void k_clear_pending(uint32_t* m0, uint32_t* m1, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    m0[i] &= ~META_PENDING;
+    m1[i] &= ~META_PENDING;
+  }
+}
+
+// Resident CTAs per SM the period kernel is compiled for: 7 x 152 SMs hold
+// the 1,024 chunks of 65,536 particles with 72 registers per thread.
+#ifndef RD_PERIOD_MIN_BLOCKS
+#define RD_PERIOD_MIN_BLOCKS 7
+#endif
+
+template <int D, int TPP>
+__global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
+    k_period(const __grid_constant__ Args d0, const __grid_constant__ Args d1,
+             const __grid_constant__ Args r0, const __grid_constant__ Args r1, PeriodArgs p) {
+  constexpr int PER = LBLOCK / TPP;
+  __shared__ PeriodShared ps;
+  __shared__ float sacc[3][PER];
+  // No early launch of the next kernel: its CTAs must not take the SM slots
+  // that CTAs of this kernel still wait for.
+  const Chunk ch = chunk_at<PER>(d0, (int)blockIdx.x);
+  list_tables<true, true, true>(ps.sh, d0, ch);
+  pdl_wait();
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    ps.s0 = d0.step_base ? *d0.step_base + d0.step : d0.step;
+    if (blockIdx.x == 0) {
+      // the candidate lists of the per-step kernels stay empty
+      d0.rx_count[0] = 0;
+      d0.rx_count[1] = 0;
+      d0.rx_count[2] = 0;
+    }
+  }
+  if (tid < CAND_WORDS) {
+    ps.cmask[0][tid] = p.rx ? d0.cand0[blockIdx.x * CAND_WORDS + tid] : 0u;
+    ps.cmask[1][tid] = 0u;
+  }
+  // the wait list: the bitmap's chunks other than this one, in order
+  if (tid < 32) {
+    int base = 0;
+    for (int w0 = 0; w0 < PMASK_WORDS; w0 += 32) {
+      const int w = w0 + tid;
+      uint32_t bits = w < PMASK_WORDS ? d0.nbmask[(size_t)blockIdx.x * PMASK_WORDS + w] : 0u;
+      if (w == (int)(blockIdx.x >> 5)) bits &= ~(1u << (blockIdx.x & 31));
+      const int cntw = __popc(bits);
+      int incl = cntw;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (tid >= o) incl += v;
+      }
+      int pos = base + incl - cntw;
+      for (uint32_t b = bits; b; b &= b - 1u) ps.wl[pos++] = (unsigned short)(w * 32 + __ffs(b) - 1);
+      base += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (tid == 0) ps.nwl = base;
+  }
+  __syncthreads();
+  const long long slot = d0.stamps ? (ps.s0 / p.nsteps) % d0.stamp_ring : 0;
+  if (d0.stamps && tid == 0)
+    d0.stamps[((size_t)slot * gridDim.x + blockIdx.x) * 2] = global_timer();
+  for (int n = 0; n < p.nsteps; n += 2) {
+    if (!period_run_step<D, TPP, 0>(ps, sacc, d0, r0, p, ch, n)) return;
+    if (n + 1 < p.nsteps && !period_run_step<D, TPP, 1>(ps, sacc, d1, r1, p, ch, n + 1)) return;
+  }
+  if (d0.stamps && (tid & 31) == 0)
+    atomicMax(d0.stamps + ((size_t)slot * gridDim.x + blockIdx.x) * 2 + 1, global_timer());
 }
 
 }  // namespace rd

@@ -23,7 +23,7 @@ EXPORTS = [
     "rdsim_get_step", "rdsim_set_step", "rdsim_set_trajectory", "rdsim_get_trajectory",
     "rdsim_get_error", "rdsim_get_stream", "rdsim_get_info", "rdsim_last_error",
     "rdsim_set_profiling", "rdsim_get_profile", "rdsim_get_pairs_static",
-    "rdsim_get_observables", "rdsim_get_rdf",
+    "rdsim_get_observables", "rdsim_get_rdf", "rdsim_test_withhold",
 ]
 
 
@@ -69,6 +69,7 @@ def load_library(path=None):
     L.rdsim_get_info.argtypes = [vp, C.POINTER(abi.Info)]
     L.rdsim_set_profiling.argtypes = [vp, C.c_int32]
     L.rdsim_get_profile.argtypes = [vp, C.POINTER(abi.Profile)]
+    L.rdsim_test_withhold.argtypes = [vp, C.c_int32]
     L.rdsim_last_error.restype = C.c_char_p
     if path is None:
         _lib = L
@@ -107,7 +108,8 @@ class Engine:
     """
 
     def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, use_graphs=True,
-                 list_width=0, reaction_prefilter=None, autotune=False, precision="float32"):
+                 list_width=0, reaction_prefilter=None, autotune=False, precision="float32",
+                 period_kernel=True, sync_wait_ms=0):
         """``autotune=True`` picks ``skin`` and ``threads_per_particle`` by
         timing short runs of this batch (:mod:`pyrdsim_gb300.autotune`,
         cached per workload).  ``precision="float64"`` evaluates pair and
@@ -136,6 +138,8 @@ class Engine:
         opt.use_graphs = 0 if use_graphs else -1
         opt.list_width = list_width
         opt.force_precision = 1 if precision == "float64" else 0
+        opt.period_kernel = 0 if period_kernel else -1
+        opt.sync_wait_ms = int(sync_wait_ms)
         # None: automatic; True: whenever the rates allow; False: off
         opt.reaction_prefilter = 0 if reaction_prefilter is None else (1 if reaction_prefilter else -1)
         h = C.c_void_p()
@@ -310,6 +314,11 @@ class Engine:
         s = C.c_void_p()
         _check(self.lib.rdsim_get_stream(self.h, C.byref(s)))
         return s.value
+
+    def test_withhold(self, chunk):
+        """Test hook: chunk ``chunk`` of the period kernel stops publishing
+        its progress (its neighbours' waits run out); -1 restores."""
+        _check(self.lib.rdsim_test_withhold(self.h, int(chunk)))
 
     def set_profiling(self, on=True, stamps=False):
         """``on``: CUDA events around every launch (serialised, no graphs);

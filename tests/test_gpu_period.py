@@ -1,0 +1,100 @@
+"""The period kernel (one launch per graph-replayed rebuild period, CTAs
+synchronised by the progress words of neighbouring chunks) against the
+per-step drift and reaction kernels it replaces: identical states bit for bit
+(same per-particle arithmetic), and a wait that runs out ends the call with
+RDSIM_ERR_SYNC instead of hanging the GPU."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import _case, _engine
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(case):
+    from pyrdsim_gb300 import workloads
+    if case == "active_wall_fluid_65536":
+        # fast reactions: several listed draws per chunk and step
+        return [workloads.active_wall_fluid(n=65536, seed=5, k_on=2.0, k_off=5.0)]
+    if case == "active_wall_fluid_rx":
+        return [workloads.active_wall_fluid(n=4096, seed=7, k_on=20.0, k_off=50.0)]
+    if case == "patchy_colloids":
+        return [workloads.patchy_colloids(n_molecules=2048, seed=3)]
+    if case == "lj_fluid":
+        return [workloads.lj_fluid(n=1024, seed=1, start="lattice")]
+    if case == "ensemble":
+        return workloads.ensemble(n_systems=8, n_min=256, n_max=4096, seed=11)
+    return [_case(case)[1]]
+
+
+CASES = ["active_wall_fluid_65536", "active_wall_fluid_rx", "patchy_colloids", "lj_fluid",
+         "ensemble", "two_species_wall_rx", "patchy", "mixed_laws", "lj3d"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_period_kernel_is_bit_identical(case):
+    """Positions, types and drift equal those of the per-step kernels after
+    calls that start, split and end rebuild periods."""
+    sds = _workload(case)
+    one = _engine(sds)
+    per_step = _engine(sds, period_kernel=False)
+    assert one.info()["period_kernel"] == 1, one.info()
+    assert per_step.info()["period_kernel"] == 0
+    prev = one.state()[1]
+    changed = 0
+    for n in (5, 33, 64, 1, 97):
+        one.step(n)
+        per_step.step(n)
+        xa, ta = one.state()
+        xb, tb = per_step.state()
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(xa, xb)
+        changed += int((ta != prev).sum())
+        prev = ta
+    np.testing.assert_array_equal(one.drift(), per_step.drift())
+    if case in ("active_wall_fluid_65536", "active_wall_fluid_rx", "two_species_wall_rx"):
+        assert changed >= 5, "too few reactions to exercise the listed draws"
+
+
+def test_period_kernel_replaces_the_step_launches():
+    """A replayed period is six launches (five rebuild kernels and the period
+    kernel) instead of five plus two per step."""
+    from pyrdsim_gb300 import workloads
+    sd = workloads.active_wall_fluid(n=8192, seed=3)
+    e = _engine([sd])
+    e.step(9)  # reach the start of a period
+    e.profile()
+    e.step(41)  # steps 10..50
+    prof = e.profile()
+    # periods 10, 20, 30 and 40 replayed (one period kernel each), the last
+    # step 50 by its own drift kernel
+    assert prof["force"]["launches"] == 4 + 1, prof
+
+
+def test_period_wait_runs_out_without_hanging():
+    """A chunk that never publishes its progress makes its neighbours' waits
+    end after the limit: the call returns RDSIM_ERR_SYNC, the handle stays
+    usable, and once restored it steps like a fresh handle."""
+    from pyrdsim_gb300 import abi, workloads
+    from pyrdsim_gb300.engine import EngineError
+    sd = workloads.active_wall_fluid(n=8192, seed=3)
+    e = _engine([sd], sync_wait_ms=20)
+    x0, t0 = e.state()
+    e.step(9)
+    e.test_withhold(5)
+    with pytest.raises(EngineError) as ei:
+        e.step(25)
+    assert ei.value.code == abi.ERR_SYNC, str(ei.value)
+    assert "waited longer" in str(ei.value)
+    e.test_withhold(-1)
+    e.set_state(x0, t0)
+    e.step_index = 0
+    ref = _engine([sd])
+    ref.set_state(x0, t0)  # the same float64 round trip of the state
+    for n in (9, 25):
+        e.step(n)
+        ref.step(n)
+    xa, ta = e.state()
+    xb, tb = ref.state()
+    np.testing.assert_array_equal(ta, tb)
+    np.testing.assert_array_equal(xa, xb)
