@@ -137,6 +137,28 @@ __host__ __device__ inline bool fixed_from_double(double x, double L, bool perio
   return true;
 }
 
+// Words that other CTAs of a running period kernel write (positions and
+// type words of other particles) are read there with strong relaxed loads
+// (coherent at GPU scope, not cached in L1), so that no acquire fence has
+// to invalidate the SM's L1, which holds the list rows and the CTA's own
+// words.  Elsewhere plain loads.  RD_PERIOD_CG: 0 plain loads after an
+// acquire fence, 1 ld.global.cg, 2 ld.relaxed.gpu.
+#ifndef RD_PERIOD_CG
+#define RD_PERIOD_CG 2
+#endif
+__device__ inline uint32_t ldw(const Args& a, const uint32_t* p) {
+#if RD_PERIOD_CG == 1
+  if (a.flags & F_PERIOD) return __ldcg(p);
+#elif RD_PERIOD_CG == 2
+  if (a.flags & F_PERIOD) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+  }
+#endif
+  return *p;
+}
+
 // Distance of two particles exactly as pyrdsim.pyx:1619-1633 computes it
 // (float64, C round() minimum image, pow(v, 2) summed in dimension order).
 template <int D>
@@ -144,8 +166,8 @@ __device__ double exact_dist(const SysDev& s, const Args& a, int gi, int gj) {
   double d2 = 0.0;
 #pragma unroll
   for (int k = 0; k < D; k++) {
-    double xi = fixed_to_double(s, k, a.xh[k][gi], a.xl[k][gi]);
-    double xj = fixed_to_double(s, k, a.xh[k][gj], a.xl[k][gj]);
+    double xi = fixed_to_double(s, k, ldw(a, a.xh[k] + gi), ldw(a, a.xl[k] + gi));
+    double xj = fixed_to_double(s, k, ldw(a, a.xh[k] + gj), ldw(a, a.xl[k] + gj));
     double v = __dsub_rn(xj, xi);
     // minimum image; round(v / L) is 0 whenever |v| < 0.49 L, which holds for
     // every pair of adjacent cells except in boxes of three cells or fewer
@@ -194,8 +216,8 @@ __device__ inline float u128_to_float(unsigned __int128 v) {
 // (minimum image in periodic dimensions), rounded once to float32 before the
 // unit is applied: bonded terms, whose partners may lie anywhere in the box.
 __device__ inline float disp_full(const SysDev& s, const Args& a, int k, int gi, int gj) {
-  const unsigned long long Xi = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
-  const unsigned long long Xj = ((unsigned long long)a.xh[k][gj] << 32) | a.xl[k][gj];
+  const unsigned long long Xi = ((unsigned long long)ldw(a, a.xh[k] + gi) << 32) | ldw(a, a.xl[k] + gi);
+  const unsigned long long Xj = ((unsigned long long)ldw(a, a.xh[k] + gj) << 32) | ldw(a, a.xl[k] + gj);
   return __ll2float_rn((long long)(Xj - Xi)) * s.unitf[k];
 }
 
@@ -362,9 +384,9 @@ __device__ inline void gaussians(const U4& w, float* xi) {
 // periodic dimensions, a reflection at 0 and L in reflecting ones, where X
 // lies in [-S, S] (S = 2^62), so X + d and the reflections stay within
 // int64.  Writes the high, low and pair words.
-__device__ inline void advance(const SysDev& s, const Args& a, int gi, int pid, int k,
-                               long long d, long long em_step) {
-  unsigned long long X = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
+// X: the coordinate's current fixed-point value.
+__device__ inline void advance_x(const SysDev& s, const Args& a, int gi, int pid, int k,
+                                 long long d, long long em_step, unsigned long long X) {
   if ((s.periodic >> k) & 1) {
     X += (unsigned long long)d;
   } else {
@@ -388,15 +410,32 @@ __device__ inline void advance(const SysDev& s, const Args& a, int gi, int pid, 
   a.xp_out[k][gi] = (uint32_t)(X >> s.ps[k]);
 }
 
+__device__ inline void advance(const SysDev& s, const Args& a, int gi, int pid, int k,
+                               long long d, long long em_step) {
+  advance_x(s, a, gi, pid, k, d, em_step,
+            ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi]);
+}
+
+// The words of one particle that its per-particle tail reads, loaded by the
+// caller: current high and low words, high words at the last rebuild, and
+// (optionally) its standard normals of the update.
+struct TailIn {
+  uint32_t xh[3], xl[3], xr[3];
+  const float* xi;                // nullptr: drawn from w0 / Philox / xi buffer
+};
+
 // Euler-Maruyama update + boundary conditions of one particle in fixed point
 // (pyrdsim.pyx:2240-2292): x += dt D a + sqrt(2 dt D) xi, then reflect or wrap.
 template <int D>
-__device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid, int type,
-                                 const float* acc, long long em_step, int flags,
-                                 const U4* w0 = nullptr) {
+__device__ inline void em_update_in(const SysDev& s, const Args& a, int gi, int pid, int type,
+                                    const float* acc, long long em_step, int flags,
+                                    const U4* w0, const TailIn& t) {
   float xi[3] = {0.f, 0.f, 0.f};
   if (!(flags & F_NO_NOISE)) {
-    if (flags & F_INJECT) {
+    if (t.xi) {
+#pragma unroll
+      for (int k = 0; k < D; k++) xi[k] = t.xi[k];
+    } else if (flags & F_INJECT) {
 #pragma unroll
       for (int k = 0; k < D; k++) xi[k] = (float)a.xi[(size_t)pid * D + k];
     } else {
@@ -410,8 +449,28 @@ __device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid
     float dl = fp * acc[k] + np * xi[k];
     long long d = delta_fixed(dl, s.inv_unit_hi[k], &bad);
     if (bad) record_error(a.err, RDSIM_ERR_NONFINITE, pid, k, (double)dl, em_step);
-    advance(s, a, gi, pid, k, d, em_step);
+    advance_x(s, a, gi, pid, k, d, em_step, ((unsigned long long)t.xh[k] << 32) | t.xl[k]);
   }
+}
+
+template <int D>
+__device__ inline TailIn tail_load(const Args& a, int gi) {
+  TailIn t;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    t.xh[k] = k < D ? a.xh[k][gi] : 0u;
+    t.xl[k] = k < D ? a.xl[k][gi] : 0u;
+    t.xr[k] = k < D ? a.xr[k][gi] : 0u;
+  }
+  t.xi = nullptr;
+  return t;
+}
+
+template <int D>
+__device__ inline void em_update(const SysDev& s, const Args& a, int gi, int pid, int type,
+                                 const float* acc, long long em_step, int flags,
+                                 const U4* w0 = nullptr) {
+  em_update_in<D>(s, a, gi, pid, type, acc, em_step, flags, w0, tail_load<D>(a, gi));
 }
 
 // ---------------------------------------------------------------------------
@@ -444,7 +503,8 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
 #pragma unroll
         for (int k = 0; k < D; k++) {
           const unsigned long long Xi = ((unsigned long long)a.xh[k][gi] << 32) | a.xl[k][gi];
-          const unsigned long long Xj = ((unsigned long long)a.xh[k][other] << 32) | a.xl[k][other];
+          const unsigned long long Xj =
+              ((unsigned long long)ldw(a, a.xh[k] + other) << 32) | ldw(a, a.xl[k] + other);
           const long long dd = (long long)(Xj - Xi);
           const unsigned long long m = dd < 0 ? 0ull - (unsigned long long)dd : (unsigned long long)dd;
           S2 += (unsigned __int128)m * m;
@@ -524,9 +584,10 @@ __device__ inline void bonded_terms(const SysDev& s, const Args& a, int gi, int 
 // (pyrdsim.pyx:1979-1986), bonded terms, drift store, finiteness and skin
 // checks, and the fused Euler-Maruyama update.  acc holds the pair drift.
 template <int D>
-__device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const Args& a, int gi,
-                                  int pid, const uint32_t* xo_h, uint32_t mi, float* acc,
-                                  const U4* w0 = nullptr) {
+__device__ inline void force_tail_in(const SysDev& s, const WallLaw* walls, const Args& a, int gi,
+                                     int pid, const TailIn& t, uint32_t mi, float* acc,
+                                     const U4* w0 = nullptr) {
+  const uint32_t* xo_h = t.xh;
   const int ti = mi & 0xff;
   // walls (pyrdsim.pyx:1979-1986)
   for (int w = 0; w < s.nwalls; w++) {
@@ -543,19 +604,23 @@ __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const A
       f = W.c0 * 4.0f * e / ((1.0f + e) * (1.0f + e));
     } else {
       // the high word alone first (it is at most the coordinate): all but
-      // the particles near the wall stop here without reading the low word
+      // the particles near the wall stop here
       const float yh = (((s.periodic >> W.dim) & 1) ? (float)h : (float)(int)h) *
                        s.unit_hi[W.dim];
       if (yh > W.rc_hi) continue;
       // the full coordinate; reflecting ones are signed (an initial
       // position may lie below 0)
-      const unsigned long long X = ((unsigned long long)h << 32) | a.xl[W.dim][gi];
+      uint32_t l = t.xl[0];
+#pragma unroll
+      for (int k = 1; k < D; k++)
+        if (k == W.dim) l = t.xl[k];
+      const unsigned long long X = ((unsigned long long)h << 32) | l;
       const float y = (((s.periodic >> W.dim) & 1) ? __ull2float_rn(X)
                                                     : __ll2float_rn((long long)X)) *
                       s.unitf[W.dim];
       if (y > W.rc_hi) continue;
       if (y >= W.rc_lo) {
-        const double yd = fixed_to_double(s, W.dim, h, a.xl[W.dim][gi]);
+        const double yd = fixed_to_double(s, W.dim, h, l);
         if (yd > W.rc) continue;
       }
       const float sr = W.c1 / y, s3 = sr * sr * sr, s9 = s3 * s3 * s3;
@@ -580,13 +645,24 @@ __device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const A
     float rel2 = 0.f;
 #pragma unroll
     for (int k = 0; k < D; k++) {
-      const float rel = (float)(int)(xo_h[k] - a.xr[k][gi]) * s.unit_hi[k];
+      const float rel = (float)(int)(xo_h[k] - t.xr[k]) * s.unit_hi[k];
       rel2 += rel * rel;
     }
     if (rel2 > s.delta * s.delta)
       record_error(a.err, RDSIM_ERR_SKIN, pid, -1, (double)sqrtf(rel2), eff_step(a));
   }
-  if (a.flags & F_EM) em_update<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags, w0);
+  if (a.flags & F_EM) em_update_in<D>(s, a, gi, pid, ti, acc, eff_em_step(a), a.flags, w0, t);
+}
+
+// The same with the words loaded here (xo_h: the current high words).
+template <int D>
+__device__ inline void force_tail(const SysDev& s, const WallLaw* walls, const Args& a, int gi,
+                                  int pid, const uint32_t* xo_h, uint32_t mi, float* acc,
+                                  const U4* w0 = nullptr) {
+  TailIn t = tail_load<D>(a, gi);
+#pragma unroll
+  for (int k = 0; k < D; k++) t.xh[k] = xo_h[k];
+  force_tail_in<D>(s, walls, a, gi, pid, t, mi, acc, w0);
 }
 
 // ---------------------------------------------------------------------------

@@ -299,8 +299,8 @@ __device__ inline Nb gather(const Args& a, int v) {
   const int j = v & 0x7fffffff;
   n.v = v;
 #pragma unroll
-  for (int k = 0; k < 3; k++) n.x[k] = k < D ? a.xp[k][j] : 0u;
-  n.m = a.meta[j];
+  for (int k = 0; k < 3; k++) n.x[k] = k < D ? (PEND ? ldw(a, a.xp[k] + j) : a.xp[k][j]) : 0u;
+  n.m = PEND ? ldw(a, a.meta + j) : a.meta[j];
   if (PEND && (n.m & META_PENDING)) n.m = wait_final_meta(a, j, n.m);
   return n;
 }
@@ -946,8 +946,13 @@ __device__ inline int ld_poll(const int* p) {
   return v;
 }
 
+// With RD_PERIOD_CG the words written by other CTAs are read from L2 and
+// the relaxed poll that saw a chunk's progress precedes those reads (they
+// issue only after the poll's loop has exited on the value, and the writer
+// fenced its words before publishing): no fence here, and the SM's L1 keeps
+// the list rows.
 __device__ inline void fence_acquire() {
-#if !RD_PERIOD_POLL_ACQUIRE
+#if !RD_PERIOD_POLL_ACQUIRE && !RD_PERIOD_CG
   asm volatile("fence.acq_rel.gpu;" ::: "memory");
 #endif
 }
@@ -955,6 +960,20 @@ __device__ inline void fence_acquire() {
 __device__ inline void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+
+// Per-particle words of the chunk staged in shared memory by the tail
+// threads: static ones once per period (caller index, high words at the
+// rebuild), the CTA's own positions and the noise of the coming update
+// before each step's wait (they depend on no other chunk).
+template <int PER>
+struct PeriodStage {
+  int pid[PER];
+  uint32_t xr[3][PER];
+  uint32_t xh[3][PER];
+  uint32_t xl[3][PER];
+  uint32_t w[4][PER];               // Philox words of the update (tag 0)
+  float xi[3][PER];                 // their standard normals
+};
 
 struct PeriodShared {
   ListShared sh;
@@ -1022,11 +1041,37 @@ __device__ __noinline__ void period_resolve(const ListShared& sh, const Args& r,
 // Step n of the period on the CTA's chunk: d / r are the step arguments of
 // the drift and of the reactions (buffers of parity P = n & 1).
 template <int D, int TPP, int P>
-__device__ __forceinline__ bool period_run_step(PeriodShared& ps, float (*sacc)[LBLOCK / TPP],
+__device__ __forceinline__ bool period_run_step(PeriodShared& ps,
+                                                PeriodStage<LBLOCK / TPP>& st,
+                                                float (*sacc)[LBLOCK / TPP],
                                                 const Args& d, const Args& r,
                                                 const PeriodArgs& p, const Chunk& ch, int n) {
   const int tid = threadIdx.x, warp = tid >> 5, l32 = tid & 31;
   const SysDev& s = ps.sh.sys;
+  const bool rx_next = p.rx && n + 1 < p.nsteps;
+  const bool words = rx_next || !(d.flags & F_NO_NOISE);
+  // the tail thread's own words and noise, while other chunks finish
+  if (tid < ch.cnt) {
+    const int ib = ch.beg + tid;
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      st.xh[k][tid] = d.xh[k][ib];
+      st.xl[k][tid] = d.xl[k][ib];
+    }
+    if (words) {
+      const U4 w0 = noise_words(s.seed, ps.s0 + n + 1, st.pid[tid], 0u);
+      st.w[0][tid] = w0.x;
+      st.w[1][tid] = w0.y;
+      st.w[2][tid] = w0.z;
+      st.w[3][tid] = w0.w;
+      if (!(d.flags & F_NO_NOISE)) {
+        float xi[3];
+        gaussians<D>(w0, xi);
+#pragma unroll
+        for (int k = 0; k < D; k++) st.xi[k][tid] = xi[k];
+      }
+    }
+  }
   if (tid == 0) period_step = ps.s0 + n;
   if (!period_wait(ps, d.pflag, n, p, d.err, ps.s0 + n)) return false;
   // reactions of step n: the chunk's listed particles, a warp each
@@ -1051,12 +1096,6 @@ __device__ __forceinline__ bool period_run_step(PeriodShared& ps, float (*sacc)[
   const int g = tid / TPP, lane = tid % TPP;
   const bool active = g < ch.cnt;
   const int i = ch.beg + (active ? g : 0);
-  if (tid < ch.cnt) {
-    const int ib = ch.beg + tid;
-    prefetch_l1(d.pid + ib);
-#pragma unroll
-    for (int k = 0; k < D; k++) prefetch_l1(d.xl[k] + ib);
-  }
   const int cnt = d.ncnt[i];
   uint32_t xo[3] = {0u, 0u, 0u};
 #pragma unroll
@@ -1075,22 +1114,27 @@ __device__ __forceinline__ bool period_run_step(PeriodShared& ps, float (*sacc)[
     for (int k = 0; k < D; k++) sacc[k][g] = acc[k];
   }
   __syncthreads();
-  const bool rx_next = p.rx && n + 1 < p.nsteps;
   const int ib = ch.beg + tid;
   bool listed = false;
   if (tid < ch.cnt) {
-    uint32_t xb[3] = {0u, 0u, 0u};
+    TailIn t;
+    float xi[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < D; k++) xb[k] = d.xh[k][ib];
+    for (int k = 0; k < 3; k++) {
+      t.xh[k] = k < D ? st.xh[k][tid] : 0u;
+      t.xl[k] = k < D ? st.xl[k][tid] : 0u;
+      t.xr[k] = k < D ? st.xr[k][tid] : 0u;
+      if (k < D && !(d.flags & F_NO_NOISE)) xi[k] = st.xi[k][tid];
+    }
+    t.xi = xi;
     float accb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < D; k++) accb[k] = sacc[k][tid];
     const uint32_t mb = d.meta[ib];
-    const int pid = d.pid[ib];
-    const bool words = rx_next || !(d.flags & F_NO_NOISE);
+    const int pid = st.pid[tid];
     U4 w0 = {0u, 0u, 0u, 0u};
-    if (words) w0 = noise_words(s.seed, ps.s0 + n + 1, pid, 0u);
-    force_tail<D>(s, ps.sh.walls, d, ib, pid, xb, mb, accb, words ? &w0 : nullptr);
+    if (words) w0 = U4{st.w[0][tid], st.w[1][tid], st.w[2][tid], st.w[3][tid]};
+    force_tail_in<D>(s, ps.sh.walls, d, ib, pid, t, mb, accb, words ? &w0 : nullptr);
     if (rx_next) {
       listed = rx_may_react<D>(s, (int)(mb & 0xff), d.ncnt[ib], pid, ps.s0 + n + 1, &w0);
       // the next step's type word, marked while its draw is pending
@@ -1126,6 +1170,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
              const __grid_constant__ Args r0, const __grid_constant__ Args r1, PeriodArgs p) {
   constexpr int PER = LBLOCK / TPP;
   __shared__ PeriodShared ps;
+  __shared__ PeriodStage<PER> st;
   __shared__ float sacc[3][PER];
   // No early launch of the next kernel: its CTAs must not take the SM slots
   // that CTAs of this kernel still wait for.
@@ -1145,6 +1190,12 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
   if (tid < CAND_WORDS) {
     ps.cmask[0][tid] = p.rx ? d0.cand0[blockIdx.x * CAND_WORDS + tid] : 0u;
     ps.cmask[1][tid] = 0u;
+  }
+  if (tid < ch.cnt) {  // static for the period
+    const int ib = ch.beg + tid;
+    st.pid[tid] = d0.pid[ib];
+#pragma unroll
+    for (int k = 0; k < D; k++) st.xr[k][tid] = d0.xr[k][ib];
   }
   // the wait list: the bitmap's chunks other than this one, in order
   if (tid < 32) {
@@ -1171,8 +1222,8 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
   if (d0.stamps && tid == 0)
     d0.stamps[((size_t)slot * gridDim.x + blockIdx.x) * 2] = global_timer();
   for (int n = 0; n < p.nsteps; n += 2) {
-    if (!period_run_step<D, TPP, 0>(ps, sacc, d0, r0, p, ch, n)) return;
-    if (n + 1 < p.nsteps && !period_run_step<D, TPP, 1>(ps, sacc, d1, r1, p, ch, n + 1)) return;
+    if (!period_run_step<D, TPP, 0>(ps, st, sacc, d0, r0, p, ch, n)) return;
+    if (n + 1 < p.nsteps && !period_run_step<D, TPP, 1>(ps, st, sacc, d1, r1, p, ch, n + 1)) return;
   }
   if (d0.stamps && (tid & 31) == 0)
     atomicMax(d0.stamps + ((size_t)slot * gridDim.x + blockIdx.x) * 2 + 1, global_timer());
