@@ -166,7 +166,15 @@ typedef struct {
                                      and one reaction launch per step        */
   int32_t sync_wait_ms;           /* limit of one wait of the period kernel on
                                      its neighbouring chunks; <= 0: 1000 ms   */
-  int32_t reserved[3];
+  int32_t list_period;            /* steps between the engine's neighbour-list
+                                     rebuilds; <= 0: the deck's
+                                     neighbor_list_update_frequency.  The
+                                     automatic skin covers the diffusion of
+                                     one period and the displacement check
+                                     keeps every pair in range listed, so the
+                                     forces do not depend on it (float32 sums
+                                     in another order)                       */
+  int32_t reserved[2];
 } rdsim_options;
 
 /* rdsim_step flags */

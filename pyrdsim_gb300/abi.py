@@ -111,7 +111,8 @@ class Options(C.Structure):
                 ("threads_per_particle", C.c_int32), ("force_precision", C.c_int32),
                 ("use_graphs", C.c_int32), ("list_width", C.c_int32),
                 ("reaction_prefilter", C.c_int32), ("period_kernel", C.c_int32),
-                ("sync_wait_ms", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("sync_wait_ms", C.c_int32), ("list_period", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class Info(C.Structure):

@@ -1,11 +1,13 @@
 """Autotuner of the engine's launch geometry for a given batch of systems.
 
-Two options set how the step kernels map onto the GPU: the Verlet skin
+Three options set how the step kernels map onto the GPU: the Verlet skin
 (``skin``: twice the displacement allowed between list rebuilds; with the
-interaction range it sets the cell size and the list radius) and the lanes
-that share one particle's list (``threads_per_particle``: 1, 2, 4 or 8).  A
-larger skin means longer lists but cheaper rebuild bookkeeping; more lanes
-mean more parallelism per particle but more shuffle traffic.  Neither
+interaction range it sets the cell size and the list radius), the lanes
+that share one particle's list (``threads_per_particle``: 1, 2, 4 or 8) and
+the steps between list rebuilds (``list_period``; the automatic skin grows
+with it).  A larger skin means longer lists but cheaper rebuild
+bookkeeping; more lanes mean more parallelism per particle but more shuffle
+traffic; a longer period means fewer rebuilds and longer lists.  None
 changes the physics (results agree within float32 summation order).
 
 :func:`autotune` times short Philox-noise runs of every candidate on the
@@ -27,6 +29,8 @@ LANES = (1, 2, 4, 8)
 # wide margin; smaller skins can fail the displacement check on long runs, so
 # only larger ones (longer lists, larger cells) are tried.
 SKIN_FACTORS = (1.0, 1.25, 1.5)
+# List periods tried, as multiples of the deck's neighbor_list_update_frequency.
+PERIOD_FACTORS = (2, 4)
 
 
 def default_cache_path():
@@ -70,7 +74,8 @@ def _time_engine(systems, device, opts, steps):
     except EngineError:
         return 0.0
     try:
-        freq = max(1, systems[0].model.neighbor_list_update_frequency)
+        freq = max(1, systems[0].model.neighbor_list_update_frequency,
+                   int(opts.get("list_period") or 0))
         eng.step(2 * freq)
         eng.state()  # synchronises the handle's stream
         t0 = time.perf_counter()
@@ -85,11 +90,13 @@ def _time_engine(systems, device, opts, steps):
 
 
 def autotune(systems, device=0, steps=200, cache_path=None, use_cache=True, measure=None):
-    """Fastest {"threads_per_particle", "skin"} for ``systems`` on ``device``.
+    """Fastest {"threads_per_particle", "skin"[, "list_period"]} for
+    ``systems`` on ``device``.
 
     ``measure(opts) -> particle-steps/s`` replaces the timed runs (tests).
     Lane counts are tried with the automatic skin; the best lane count is
-    then tried with scaled skins.
+    then tried with scaled skins, and with longer list periods (automatic
+    skin).
     """
     from .engine import Engine
     device_name = ""
@@ -124,6 +131,14 @@ def autotune(systems, device=0, steps=200, cache_path=None, use_cache=True, meas
     best_rate, best = max(results, key=lambda r: r[0])
     for opts in candidates(auto_skin)[len(LANES):]:
         o = dict(opts, threads_per_particle=best["threads_per_particle"])
+        rate = measure(dict(o))
+        results.append((rate, o))
+        if rate > best_rate:
+            best_rate, best = rate, o
+    freq = max(1, systems[0].model.neighbor_list_update_frequency)
+    lanes = best["threads_per_particle"]
+    for f in PERIOD_FACTORS:
+        o = {"threads_per_particle": lanes, "skin": 0.0, "list_period": int(f * freq)}
         rate = measure(dict(o))
         results.append((rate, o))
         if rate > best_rate:

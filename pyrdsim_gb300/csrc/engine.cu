@@ -786,8 +786,8 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     if (S.n_interactions > MAXI) return bail(fail(RDSIM_ERR_UNSUPPORTED, "at most 32 interactions per system"));
     if (S.n_reactions > MAXR) return bail(fail(RDSIM_ERR_UNSUPPORTED, "at most 8 reactions per system"));
     if (S.neighbor_list_update_frequency <= 0) return bail(fail(RDSIM_ERR_ARG, "neighbor_list_update_frequency must be positive"));
-    if (si == 0) h->freq = S.neighbor_list_update_frequency;
-    else if (S.neighbor_list_update_frequency != h->freq)
+    if (si == 0) h->freq = opt.list_period > 0 ? opt.list_period : S.neighbor_list_update_frequency;
+    else if (S.neighbor_list_update_frequency != systems[0].neighbor_list_update_frequency)
       return bail(fail(RDSIM_ERR_UNSUPPORTED, "batched systems must share neighbor_list_update_frequency"));
     SysDev sd;
     std::memset(&sd, 0, sizeof sd);

@@ -109,7 +109,7 @@ class Engine:
 
     def __init__(self, systems, device=0, skin=0.0, threads_per_particle=0, use_graphs=True,
                  list_width=0, reaction_prefilter=None, autotune=False, precision="float32",
-                 period_kernel=True, sync_wait_ms=0):
+                 period_kernel=True, sync_wait_ms=0, list_period=0):
         """``autotune=True`` picks ``skin`` and ``threads_per_particle`` by
         timing short runs of this batch (:mod:`pyrdsim_gb300.autotune`,
         cached per workload).  ``precision="float64"`` evaluates pair and
@@ -125,8 +125,9 @@ class Engine:
             best = _tune(self.systems, device=device)
             skin = best["skin"]
             threads_per_particle = best["threads_per_particle"] or 0
+            list_period = best.get("list_period", 0) or 0
         self.options = {"skin": skin, "threads_per_particle": threads_per_particle,
-                        "precision": precision}
+                        "precision": precision, "list_period": list_period}
         self.D = self.systems[0].model.N_dim
         self.offsets = np.cumsum([0] + [s.n_particles for s in self.systems])
         self.N = int(self.offsets[-1])
@@ -140,6 +141,7 @@ class Engine:
         opt.force_precision = 1 if precision == "float64" else 0
         opt.period_kernel = 0 if period_kernel else -1
         opt.sync_wait_ms = int(sync_wait_ms)
+        opt.list_period = int(list_period)
         # None: automatic; True: whenever the rates allow; False: off
         opt.reaction_prefilter = 0 if reaction_prefilter is None else (1 if reaction_prefilter else -1)
         h = C.c_void_p()
