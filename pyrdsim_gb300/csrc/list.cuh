@@ -624,30 +624,36 @@ __device__ inline int resolve_listed(const SysDev& s, const RxDev* rx, const Arg
 // Phase A of the drift kernels: this lane's share of the pair drift of
 // sorted particle i (type word mi, pair words xo) over its list entries
 // (pyrdsim.pyx:1988-2030), added to acc.
+// One list entry's pair drift on particle i (type ti, pair words xo).
+template <int D>
+__device__ __forceinline__ void pair_term(const ListShared& sh, const Args& a, int i, int ti,
+                                          const uint32_t* xo, const Nb& nb, float* acc) {
+  const SysDev& s = sh.sys;
+  if (nb.v < 0) return;  // same molecule: reactions only
+  float d[3];
+  const float r2 = pair_geom<D>(s, nb.x, xo, d);
+  const int tj = nb.m & 0xff;
+  if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
+  const unsigned int pp = s.ppair[ti * MAXT + tj];
+  const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
+  float fr;
+  if ((pp & 0x8000u) && r2 < L0.rc2_lo) {
+    // a single Lennard-Jones n = 6 law, clear of its cutoff: eval_pair's
+    // arithmetic inline
+    fr = lj6_over_r(L0.c0, L0.c1, r2, recip(r2));
+  } else {
+    fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
+  }
+#pragma unroll
+  for (int k = 0; k < D; k++) acc[k] = fmaf(fr, d[k], acc[k]);
+}
+
 template <int D, int TPP, bool PEND = false>
 __device__ __forceinline__ void pair_drift(const ListShared& sh, const Args& a, int i, int lane,
                                            int cnt, const uint32_t* xo, uint32_t mi, float* acc) {
-  const SysDev& s = sh.sys;
   const int ti = mi & 0xff;
-  for_entries<D, TPP, PEND>(s, a, i, lane, cnt, [&](const Nb& nb) {
-    if (nb.v < 0) return;  // same molecule: reactions only
-    float d[3];
-    const float r2 = pair_geom<D>(s, nb.x, xo, d);
-    const int tj = nb.m & 0xff;
-    if (!(r2 < s.prc2[ti * MAXT + tj])) return;  // beyond every law of the pair
-    const unsigned int pp = s.ppair[ti * MAXT + tj];
-    const PairLaw& L0 = sh.laws[(pp >> 5) & 0x3ff];
-    float fr;
-    if ((pp & 0x8000u) && r2 < L0.rc2_lo) {
-      // a single Lennard-Jones n = 6 law, clear of its cutoff: eval_pair's
-      // arithmetic inline
-      fr = lj6_over_r(L0.c0, L0.c1, r2, recip(r2));
-    } else {
-      fr = pair_force<D>(s, sh.laws, a, i, nb.v, pp, r2);
-    }
-#pragma unroll
-    for (int k = 0; k < D; k++) acc[k] = fmaf(fr, d[k], acc[k]);
-  });
+  for_entries<D, TPP, PEND>(sh.sys, a, i, lane, cnt,
+                            [&](const Nb& nb) { pair_term<D>(sh, a, i, ti, xo, nb, acc); });
 }
 
 // Drift kernel.  Phase A: TPP lanes per particle sum the pair drift over its
@@ -975,6 +981,31 @@ struct PeriodStage {
   float xi[3][PER];                 // their standard normals
 };
 
+// Neighbour staging of a chunk (period kernel).  Built once per period from
+// the chunk's static list rows: per chunk that its entries touch (itself
+// included), the run [lo, hi] of sorted indices touched, laid out back to
+// back (slot -> sorted index in g); every entry of a particle whose row fits
+// (at most LS_MAX entries, none regenerated from the cells) is rewritten as
+// its slot (bit 15: same molecule).  Each step the pair and type words of
+// all slots are loaded once, coalesced, into x / m; the pair loop reads them
+// from shared memory in the list's order, so its sums are those of the
+// gathers.  A chunk whose runs exceed STAGE_MAX slots (or that touches more
+// than STAGE_CH chunks) gathers from memory as before.
+constexpr int STAGE_MAX = 384;
+constexpr int STAGE_CH = 64;
+constexpr int LS_MAX = 32;
+
+template <int D, int PER>
+struct PeriodNbStage {
+  uint32_t x[D][STAGE_MAX];
+  uint32_t m[STAGE_MAX];
+  int g[STAGE_MAX];
+  unsigned short slot[LS_MAX][PER];
+  int lo[STAGE_CH], hi[STAGE_CH], base[STAGE_CH + 1];
+  unsigned short ch[STAGE_CH];
+  int nch, total, on;
+};
+
 struct PeriodShared {
   ListShared sh;
   unsigned short wl[PMAX_CHUNKS];   // chunks waited for (not itself)
@@ -1043,6 +1074,7 @@ __device__ __noinline__ void period_resolve(const ListShared& sh, const Args& r,
 template <int D, int TPP, int P>
 __device__ __forceinline__ bool period_run_step(PeriodShared& ps,
                                                 PeriodStage<LBLOCK / TPP>& st,
+                                                PeriodNbStage<D, LBLOCK / TPP>& ns,
                                                 float (*sacc)[LBLOCK / TPP],
                                                 const Args& d, const Args& r,
                                                 const PeriodArgs& p, const Chunk& ch, int n) {
@@ -1101,9 +1133,38 @@ __device__ __forceinline__ bool period_run_step(PeriodShared& ps,
 #pragma unroll
   for (int k = 0; k < D; k++) xo[k] = d.xp[k][i];
   const uint32_t mi = d.meta[i];
-  prefetch_rows<TPP>(d, ch, cnt, active);
+  // the staged neighbours' words of this step, one coalesced pass
+  if (ns.on) {
+    for (int sl = tid; sl < ns.total; sl += LBLOCK) {
+      const int j = ns.g[sl];
+#pragma unroll
+      for (int k = 0; k < D; k++) ns.x[k][sl] = ldw(d, d.xp[k] + j);
+      ns.m[sl] = ldw(d, d.meta + j);
+    }
+    __syncthreads();
+  }
+  const bool staged = ns.on && active && cnt <= min(d.W, LS_MAX);
+  prefetch_rows<TPP>(d, ch, cnt, active && !staged);
   float acc[3] = {0.f, 0.f, 0.f};
-  if (active && s.R2 > 0.f) pair_drift<D, TPP, true>(ps.sh, d, i, lane, cnt, xo, mi, acc);
+  if (active && s.R2 > 0.f) {
+    if (staged) {
+      const int ti = mi & 0xff;
+      for (int e = lane; e < cnt; e += TPP) {
+        const unsigned int code = ns.slot[e][g];
+        const int sl = (int)(code & 0x7fffu);
+        Nb nb;
+#pragma unroll
+        for (int k = 0; k < 3; k++) nb.x[k] = k < D ? ns.x[k][sl] : 0u;
+        nb.m = ns.m[sl];
+        const int j = ns.g[sl];
+        if (nb.m & META_PENDING) nb.m = wait_final_meta(d, j, nb.m);
+        nb.v = (code & 0x8000u) ? (j | LIST_SAME_MOL) : j;
+        pair_term<D>(ps.sh, d, i, ti, xo, nb, acc);
+      }
+    } else {
+      pair_drift<D, TPP, true>(ps.sh, d, i, lane, cnt, xo, mi, acc);
+    }
+  }
 #pragma unroll
   for (int o = TPP >> 1; o > 0; o >>= 1) {
 #pragma unroll
@@ -1171,6 +1232,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
   constexpr int PER = LBLOCK / TPP;
   __shared__ PeriodShared ps;
   __shared__ PeriodStage<PER> st;
+  __shared__ PeriodNbStage<D, PER> ns;
   __shared__ float sacc[3][PER];
   // No early launch of the next kernel: its CTAs must not take the SM slots
   // that CTAs of this kernel still wait for.
@@ -1218,12 +1280,104 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
     if (tid == 0) ps.nwl = base;
   }
   __syncthreads();
+  // the neighbour staging table (PeriodNbStage)
+  {
+    const int self = (int)blockIdx.x;
+    if (tid == 0) {
+      const int n = ps.nwl;
+      int on = n + 1 <= STAGE_CH ? 1 : 0;
+      if (on) {  // the waited chunks and this one, in order
+        int o = 0;
+        bool placed = false;
+        for (int q = 0; q < n; q++) {
+          const int c = ps.wl[q];
+          if (!placed && c > self) {
+            ns.ch[o++] = (unsigned short)self;
+            placed = true;
+          }
+          ns.ch[o++] = (unsigned short)c;
+        }
+        if (!placed) ns.ch[o++] = (unsigned short)self;
+        ns.nch = o;
+      }
+      ns.on = on;
+      ns.total = 0;
+    }
+    for (int q = tid; q < STAGE_CH; q += LBLOCK) {
+      ns.lo[q] = 0x7fffffff;
+      ns.hi[q] = -1;
+    }
+    __syncthreads();
+    const SysDev& s = ps.sh.sys;
+    const int g = tid / TPP, lane = tid % TPP;
+    const int i = ch.beg + (g < ch.cnt ? g : 0);
+    const int cnt = g < ch.cnt ? d0.ncnt[i] : 0;
+    const int chunk0 = (int)blockIdx.x - (ch.beg - s.p0) / PER;
+    // position of the chunk of sorted particle j in ns.ch (-1: absent)
+    auto pos_of = [&](int j) {
+      const int h = chunk0 + (j - s.p0) / PER;
+      int lo = 0, hi = ns.nch - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)ns.ch[mid] < h) lo = mid + 1;
+        else hi = mid;
+      }
+      return (int)ns.ch[lo] == h ? lo : -1;
+    };
+    const bool mine = ns.on && g < ch.cnt && cnt <= min(d0.W, LS_MAX);
+    if (mine) {
+      for (int e = lane; e < cnt; e += TPP) {
+        const int j = d0.nbr[ell_index<TPP>(e, i, d0.npad)] & 0x7fffffff;
+        const int q = pos_of(j);
+        if (q < 0) {
+          ns.on = 0;
+          continue;
+        }
+        atomicMin(&ns.lo[q], j);
+        atomicMax(&ns.hi[q], j);
+      }
+    }
+    __syncthreads();
+    if (tid == 0 && ns.on) {
+      int b = 0;
+      for (int q = 0; q < ns.nch; q++) {
+        ns.base[q] = b;
+        if (ns.hi[q] >= ns.lo[q]) b += ns.hi[q] - ns.lo[q] + 1;
+      }
+      ns.base[ns.nch] = b;
+      ns.total = b;
+      if (b > STAGE_MAX) ns.on = 0;
+    }
+    __syncthreads();
+    if (ns.on) {
+      for (int sl = tid; sl < ns.total; sl += LBLOCK) {
+        int lo = 0, hi = ns.nch - 1;  // the last run starting at or before sl
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (ns.base[mid] <= sl) lo = mid;
+          else hi = mid - 1;
+        }
+        ns.g[sl] = ns.lo[lo] + (sl - ns.base[lo]);
+      }
+      if (mine) {
+        for (int e = lane; e < cnt; e += TPP) {
+          const int v = d0.nbr[ell_index<TPP>(e, i, d0.npad)];
+          const int j = v & 0x7fffffff;
+          const int q = pos_of(j);
+          const int sl = ns.base[q] + (j - ns.lo[q]);
+          ns.slot[e][g] = (unsigned short)(sl | (v < 0 ? 0x8000 : 0));
+        }
+      }
+    }
+    __syncthreads();
+  }
   const long long slot = d0.stamps ? (ps.s0 / p.nsteps) % d0.stamp_ring : 0;
   if (d0.stamps && tid == 0)
     d0.stamps[((size_t)slot * gridDim.x + blockIdx.x) * 2] = global_timer();
   for (int n = 0; n < p.nsteps; n += 2) {
-    if (!period_run_step<D, TPP, 0>(ps, st, sacc, d0, r0, p, ch, n)) return;
-    if (n + 1 < p.nsteps && !period_run_step<D, TPP, 1>(ps, st, sacc, d1, r1, p, ch, n + 1)) return;
+    if (!period_run_step<D, TPP, 0>(ps, st, ns, sacc, d0, r0, p, ch, n)) return;
+    if (n + 1 < p.nsteps && !period_run_step<D, TPP, 1>(ps, st, ns, sacc, d1, r1, p, ch, n + 1))
+      return;
   }
   if (d0.stamps && (tid & 31) == 0)
     atomicMax(d0.stamps + ((size_t)slot * gridDim.x + blockIdx.x) * 2 + 1, global_timer());
