@@ -35,6 +35,11 @@ METRIC = "particle-steps/s on 1 GB300 (active wall fluid, N=65,536)"
 UNIT = "particle-steps/s"
 SEGMENT = 1000
 ALG_BYTES = 40  # per particle-step: 16 B read x, 16 B write x, 4 B type read, 4 B type write
+# Steps between the engine's Verlet-list rebuilds in the timed runs (the deck
+# of the workload keeps the reference's default neighbor_list_update_frequency
+# of 10; the engine's skin grows with the period and its displacement check
+# keeps every pair in range listed, so the dynamics are the same).
+LIST_PERIOD = 20
 
 
 def parse():
@@ -162,9 +167,10 @@ def traffic_per_launch(n, steps=1, period=False):
 
 def dominant_kernel(eng, sd):
     """(kernel name, integration steps per launch) of the drift work: the
-    period kernel runs a whole rebuild period per launch."""
-    if eng.info()["period_kernel"]:
-        return "k_period<2,2>", sd.model.neighbor_list_update_frequency
+    period kernel runs a whole list period per launch."""
+    info = eng.info()
+    if info["period_kernel"]:
+        return "k_period<2,2>", int(info["list_period"])
     return "k_force_l<2,2>", 1
 
 
@@ -486,6 +492,32 @@ def lj_fluid_plain_method(local, steps=10000):
     return out
 
 
+def deck_period_value(sd, local, seg, flush, segments=6):
+    """Particle-steps/s of the headline loop (CUDA events on the engine
+    stream, L2 flushed between segments) with the engine's list period equal
+    to the deck's neighbor_list_update_frequency."""
+    import torch
+    from pyrdsim_gb300.engine import Engine
+    eng = Engine([sd], device=local)
+    stream = torch.cuda.ExternalStream(eng.stream())
+    eng.step(seg)
+    ms = 0.0
+    for _ in range(segments):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng.step(seg)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms += a.elapsed_time(b)
+    out = {"value": sd.n_particles * seg * segments / (ms / 1e3), "unit": UNIT,
+           "list_period": sd.model.neighbor_list_update_frequency, "segments": segments,
+           "ms_per_step": ms / segments}
+    eng.close()
+    return out
+
+
 def n_sweep(local, sizes=((65536, 1000), (1048576, 200), (4194304, 100))):
     """The active wall fluid at growing N (density 0.4): throughput and the
     drift kernel's average launch span (device timestamps of the timed
@@ -499,7 +531,7 @@ def n_sweep(local, sizes=((65536, 1000), (1048576, 200), (4194304, 100))):
     rows = []
     for n, steps in sizes:
         sd = workloads.active_wall_fluid(n=n)
-        eng = Engine([sd], device=local)
+        eng = Engine([sd], device=local, list_period=LIST_PERIOD)
         eng.set_profiling(False, stamps=True)
         eng.step(steps)
         eng.profile()
@@ -564,7 +596,7 @@ def run_ours(args, rank, ws, local):
     from pyrdsim_gb300.engine import Engine
     torch.cuda.set_device(local)
     sd = workloads.active_wall_fluid(n=args.n, seed=2 + rank)
-    eng = Engine([sd], device=local)
+    eng = Engine([sd], device=local, list_period=LIST_PERIOD)
     # the drift kernel stamps each CTA's start and end in the timed replays
     eng.set_profiling(False, stamps=True)
     N, seg = sd.n_particles, args.segment
@@ -636,7 +668,9 @@ def run_ours(args, rank, ws, local):
                    "integration_steps_per_step": seg, "dt": 1e-4,
                    "boundaries": "periodic x, reflecting y", "noise": "Philox4x32-10",
                    "l2": "flushed (256 MB write) between timed steps; state L2-resident "
-                         "within a step", "parallelism": f"replicas x{ws}"},
+                         "within a step", "parallelism": f"replicas x{ws}",
+                   "neighbor_list_update_frequency": sd.model.neighbor_list_update_frequency,
+                   "engine_list_period": LIST_PERIOD},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(N * 2 * 8 + N * 4),
                 "d2h_bytes_per_step": int(N * 2 * 8 + N * 4),
                 "path": "C ABI: rdsim_set_state (host) + rdsim_step + rdsim_get_state (host)"},
@@ -657,6 +691,13 @@ def run_ours(args, rank, ws, local):
         "clocks": clk,
         "engine": eng.info(),
     }
+    if rank == 0 and ws == 1:
+        # the same timed loop with the engine rebuilding at the deck's own
+        # neighbor_list_update_frequency (fewer segments)
+        try:
+            out["value_at_deck_list_period"] = deck_period_value(sd, local, seg, flush)
+        except Exception as exc:
+            out["value_at_deck_list_period"] = {"unavailable": str(exc)[:200]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         try:
             out["cpu_baseline"] = cpu_baseline("active_wall_fluid")

@@ -326,7 +326,7 @@ typedef struct {
   int32_t force_precision;        /* as in rdsim_options                      */
   int32_t period_kernel;          /* 1: rebuild periods replay as one launch of
                                      the period kernel                       */
-  int32_t pad;
+  int32_t list_period;            /* steps between Verlet-list rebuilds     */
 } rdsim_info;
 int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
 

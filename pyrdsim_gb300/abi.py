@@ -122,7 +122,7 @@ class Info(C.Structure):
                 ("cell_size_min", C.c_double), ("interaction_range", C.c_double),
                 ("device_bytes", C.c_int64), ("reaction_prefilter", C.c_int32),
                 ("force_precision", C.c_int32), ("period_kernel", C.c_int32),
-                ("pad", C.c_int32)]
+                ("list_period", C.c_int32)]
 
 
 RDF_OTHER_MOLECULES = 1

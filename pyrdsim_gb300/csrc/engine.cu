@@ -1049,11 +1049,15 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
     if (S.n_reactions > 0) h->has_rx = true;
     sd.R2 = R2;
     sd.Rrx2 = Rrx2;
-    // skin: diffusion over one rebuild period plus margin, within rs
+    // skin: diffusion over one rebuild period plus margin, within rs; at
+    // least 15 standard deviations of the period's diffusion per dimension
+    // (the allowed displacement, half the skin, then exceeds 7.5 of them: a
+    // chance below 1e-12 per particle and period)
     double sig = 0;
     for (int t = 0; t < S.n_types; t++)
       if (S.tau_by_tauD[t] > 0) sig = std::max(sig, std::sqrt(2.0 * S.dt * S.tau_by_tauD[t]));
-    double skin = opt.skin > 0 ? opt.skin : 10.0 * sig * std::sqrt((double)h->freq) + 0.05 * R + 0.1;
+    const double diff = sig * std::sqrt((double)h->freq);
+    double skin = opt.skin > 0 ? opt.skin : std::max(10.0 * diff + 0.05 * R + 0.1, 15.0 * diff);
     double delta = skin / 2;
     if (R > 0) {
       double room = (S.rs - R) / 2.0;
@@ -1858,6 +1862,7 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info) {
   info->reaction_prefilter = (h->rx_pre && h->has_rx) ? 1 : 0;
   info->force_precision = h->f64 ? 1 : 0;
   info->period_kernel = h->period_on ? 1 : 0;
+  info->list_period = h->freq;
   return 0;
 }
 

@@ -1052,10 +1052,15 @@ __device__ inline bool period_wait(PeriodShared& ps, const int* pflag, int targe
 }
 
 // Publishes progress v of the CTA's chunk; the caller has synchronised the
-// CTA after its last write of the phase.
+// CTA after its last write of the phase (the barrier orders the other
+// threads' writes before thread 0's release, which is cumulative).
+// RD_PERIOD_PUBLISH_FENCE adds a full fence before the release.
+#ifndef RD_PERIOD_PUBLISH_FENCE
+#define RD_PERIOD_PUBLISH_FENCE 0
+#endif
 __device__ inline void period_publish(int* pflag, int v, const PeriodArgs& p) {
   if (threadIdx.x == 0 && (int)blockIdx.x != p.withhold) {
-    __threadfence();
+    if (RD_PERIOD_PUBLISH_FENCE) __threadfence();
     st_release(pflag + (size_t)blockIdx.x * PFLAG_STRIDE, v);
   }
 }
