@@ -989,17 +989,18 @@ struct PeriodStage {
 // its slot (bit 15: same molecule).  Each step the pair and type words of
 // all slots are loaded once, coalesced, into x / m; the pair loop reads them
 // from shared memory in the list's order, so its sums are those of the
-// gathers.  A chunk whose runs exceed STAGE_MAX slots (or that touches more
-// than STAGE_CH chunks) gathers from memory as before.
-constexpr int STAGE_MAX = 384;
+// gathers.  A chunk whose runs exceed SMAX slots (six per particle of the
+// chunk) or that touches more than STAGE_CH chunks gathers from memory as
+// before.
 constexpr int STAGE_CH = 64;
 constexpr int LS_MAX = 32;
 
 template <int D, int PER>
 struct PeriodNbStage {
-  uint32_t x[D][STAGE_MAX];
-  uint32_t m[STAGE_MAX];
-  int g[STAGE_MAX];
+  static constexpr int SMAX = 6 * PER;
+  uint32_t x[D][SMAX];
+  uint32_t m[SMAX];
+  int g[SMAX];
   unsigned short slot[LS_MAX][PER];
   int lo[STAGE_CH], hi[STAGE_CH], base[STAGE_CH + 1];
   unsigned short ch[STAGE_CH];
@@ -1351,7 +1352,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
       }
       ns.base[ns.nch] = b;
       ns.total = b;
-      if (b > STAGE_MAX) ns.on = 0;
+      if (b > PeriodNbStage<D, PER>::SMAX) ns.on = 0;
     }
     __syncthreads();
     if (ns.on) {
