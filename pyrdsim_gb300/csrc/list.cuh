@@ -1246,8 +1246,42 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
   list_tables<true, true, true>(ps.sh, d0, ch);
   pdl_wait();
   const int tid = threadIdx.x;
+  const int g = tid / TPP, lane = tid % TPP;
+  const int i = ch.beg + (g < ch.cnt ? g : 0);
+  // every word the set-up reads (written by the list builder), issued
+  // together: one round trip instead of a chain
+  long long s0v = 0;
+  if (tid == 0) s0v = d0.step_base ? *d0.step_base + d0.step : d0.step;
+  uint32_t cw = 0u;
+  if (tid < CAND_WORDS && p.rx) cw = d0.cand0[blockIdx.x * CAND_WORDS + tid];
+  int pidv = 0;
+  uint32_t xrv[3] = {0u, 0u, 0u};
+  if (tid < ch.cnt) {
+    pidv = d0.pid[ch.beg + tid];
+#pragma unroll
+    for (int k = 0; k < D; k++) xrv[k] = d0.xr[k][ch.beg + tid];
+  }
+  uint32_t bits[2] = {0u, 0u};
+  if (tid < 32) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int w = h * 32 + tid;
+      if (w < PMASK_WORDS) bits[h] = d0.nbmask[(size_t)blockIdx.x * PMASK_WORDS + w];
+    }
+  }
+  const int cnt = g < ch.cnt ? d0.ncnt[i] : 0;
+  // this lane's entries of the row (up to the staging width, whatever the
+  // count: the ELL array holds W entries per particle)
+  constexpr int EPL = (LS_MAX + TPP - 1) / TPP;
+  const int wmax = min(d0.W, LS_MAX);
+  int ent[EPL];
+#pragma unroll
+  for (int u = 0; u < EPL; u++) {
+    const int e = lane + u * TPP;
+    ent[u] = (g < ch.cnt && e < wmax) ? d0.nbr[ell_index<TPP>(e, i, d0.npad)] : 0;
+  }
   if (tid == 0) {
-    ps.s0 = d0.step_base ? *d0.step_base + d0.step : d0.step;
+    ps.s0 = s0v;
     if (blockIdx.x == 0) {
       // the candidate lists of the per-step kernels stay empty
       d0.rx_count[0] = 0;
@@ -1256,23 +1290,23 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
     }
   }
   if (tid < CAND_WORDS) {
-    ps.cmask[0][tid] = p.rx ? d0.cand0[blockIdx.x * CAND_WORDS + tid] : 0u;
+    ps.cmask[0][tid] = cw;
     ps.cmask[1][tid] = 0u;
   }
   if (tid < ch.cnt) {  // static for the period
-    const int ib = ch.beg + tid;
-    st.pid[tid] = d0.pid[ib];
+    st.pid[tid] = pidv;
 #pragma unroll
-    for (int k = 0; k < D; k++) st.xr[k][tid] = d0.xr[k][ib];
+    for (int k = 0; k < D; k++) st.xr[k][tid] = xrv[k];
   }
   // the wait list: the bitmap's chunks other than this one, in order
   if (tid < 32) {
     int base = 0;
-    for (int w0 = 0; w0 < PMASK_WORDS; w0 += 32) {
-      const int w = w0 + tid;
-      uint32_t bits = w < PMASK_WORDS ? d0.nbmask[(size_t)blockIdx.x * PMASK_WORDS + w] : 0u;
-      if (w == (int)(blockIdx.x >> 5)) bits &= ~(1u << (blockIdx.x & 31));
-      const int cntw = __popc(bits);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int w = h * 32 + tid;
+      uint32_t bw = bits[h];
+      if (w == (int)(blockIdx.x >> 5)) bw &= ~(1u << (blockIdx.x & 31));
+      const int cntw = __popc(bw);
       int incl = cntw;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -1280,7 +1314,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
         if (tid >= o) incl += v;
       }
       int pos = base + incl - cntw;
-      for (uint32_t b = bits; b; b &= b - 1u) ps.wl[pos++] = (unsigned short)(w * 32 + __ffs(b) - 1);
+      for (uint32_t b = bw; b; b &= b - 1u) ps.wl[pos++] = (unsigned short)(w * 32 + __ffs(b) - 1);
       base += __shfl_sync(0xffffffffu, incl, 31);
     }
     if (tid == 0) ps.nwl = base;
@@ -1289,36 +1323,34 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
   // the neighbour staging table (PeriodNbStage)
   {
     const int self = (int)blockIdx.x;
-    if (tid == 0) {
-      const int n = ps.nwl;
-      int on = n + 1 <= STAGE_CH ? 1 : 0;
-      if (on) {  // the waited chunks and this one, in order
-        int o = 0;
-        bool placed = false;
-        for (int q = 0; q < n; q++) {
+    const int nwl = ps.nwl;
+    const int on0 = nwl + 1 <= STAGE_CH ? 1 : 0;
+    // the waited chunks and this one, in order (warp 0; ps.wl is sorted)
+    if (tid < 32) {
+      if (on0) {
+        int below = 0;
+        for (int q = tid; q < nwl; q += 32) {
           const int c = ps.wl[q];
-          if (!placed && c > self) {
-            ns.ch[o++] = (unsigned short)self;
-            placed = true;
-          }
-          ns.ch[o++] = (unsigned short)c;
+          below += c < self ? 1 : 0;
+          ns.ch[q + (c > self ? 1 : 0)] = (unsigned short)c;
         }
-        if (!placed) ns.ch[o++] = (unsigned short)self;
-        ns.nch = o;
+        below = __reduce_add_sync(0xffffffffu, below);
+        if (tid == 0) ns.ch[below] = (unsigned short)self;
       }
-      ns.on = on;
-      ns.total = 0;
+      if (tid == 0) {
+        ns.on = on0;
+        ns.nch = on0 ? nwl + 1 : 0;
+        ns.total = 0;
+      }
     }
     for (int q = tid; q < STAGE_CH; q += LBLOCK) {
       ns.lo[q] = 0x7fffffff;
       ns.hi[q] = -1;
     }
-    __syncthreads();
     const SysDev& s = ps.sh.sys;
-    const int g = tid / TPP, lane = tid % TPP;
-    const int i = ch.beg + (g < ch.cnt ? g : 0);
-    const int cnt = g < ch.cnt ? d0.ncnt[i] : 0;
     const int chunk0 = (int)blockIdx.x - (ch.beg - s.p0) / PER;
+    const bool mine = on0 && g < ch.cnt && cnt <= wmax;
+    __syncthreads();
     // position of the chunk of sorted particle j in ns.ch (-1: absent)
     auto pos_of = [&](int j) {
       const int h = chunk0 + (j - s.p0) / PER;
@@ -1330,10 +1362,11 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
       }
       return (int)ns.ch[lo] == h ? lo : -1;
     };
-    const bool mine = ns.on && g < ch.cnt && cnt <= min(d0.W, LS_MAX);
     if (mine) {
-      for (int e = lane; e < cnt; e += TPP) {
-        const int j = d0.nbr[ell_index<TPP>(e, i, d0.npad)] & 0x7fffffff;
+#pragma unroll
+      for (int u = 0; u < EPL; u++) {
+        if (lane + u * TPP >= cnt) break;
+        const int j = ent[u] & 0x7fffffff;
         const int q = pos_of(j);
         if (q < 0) {
           ns.on = 0;
@@ -1344,15 +1377,27 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
       }
     }
     __syncthreads();
-    if (tid == 0 && ns.on) {
-      int b = 0;
-      for (int q = 0; q < ns.nch; q++) {
-        ns.base[q] = b;
-        if (ns.hi[q] >= ns.lo[q]) b += ns.hi[q] - ns.lo[q] + 1;
+    // run lengths -> bases (warp 0, shuffle scan over at most STAGE_CH runs)
+    if (tid < 32 && ns.on) {
+      const int n = ns.nch;
+      int carry = 0;
+      for (int q0 = 0; q0 < n; q0 += 32) {
+        const int q = q0 + tid;
+        const int len = (q < n && ns.hi[q] >= ns.lo[q]) ? ns.hi[q] - ns.lo[q] + 1 : 0;
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (tid >= o) incl += v;
+        }
+        if (q < n) ns.base[q] = carry + incl - len;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
       }
-      ns.base[ns.nch] = b;
-      ns.total = b;
-      if (b > PeriodNbStage<D, PER>::SMAX) ns.on = 0;
+      if (tid == 0) {
+        ns.base[n] = carry;
+        ns.total = carry;
+        if (carry > PeriodNbStage<D, PER>::SMAX) ns.on = 0;
+      }
     }
     __syncthreads();
     if (ns.on) {
@@ -1366,8 +1411,11 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
         ns.g[sl] = ns.lo[lo] + (sl - ns.base[lo]);
       }
       if (mine) {
-        for (int e = lane; e < cnt; e += TPP) {
-          const int v = d0.nbr[ell_index<TPP>(e, i, d0.npad)];
+#pragma unroll
+        for (int u = 0; u < EPL; u++) {
+          const int e = lane + u * TPP;
+          if (e >= cnt) break;
+          const int v = ent[u];
           const int j = v & 0x7fffffff;
           const int q = pos_of(j);
           const int sl = ns.base[q] + (j - ns.lo[q]);
