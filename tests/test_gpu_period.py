@@ -134,3 +134,23 @@ def test_list_period_keeps_results(case):
         per_step.step(k)
     np.testing.assert_array_equal(one.state()[0], per_step.state()[0])
     np.testing.assert_array_equal(one.state()[1], per_step.state()[1])
+
+
+def test_period_kernel_fallbacks_are_exact():
+    """A long list period (large skin: rows longer than the 32 staged entries,
+    chunks whose neighbour runs overflow the staging table) mixes staged and
+    gathered particles within CTAs; the period kernel still equals the
+    per-step kernels bit for bit."""
+    from pyrdsim_gb300 import workloads
+    sd = workloads.active_wall_fluid(n=8192, seed=9, k_on=20.0, k_off=50.0)
+    one = _engine([sd], list_period=80)
+    per_step = _engine([sd], list_period=80, period_kernel=False)
+    assert one.info()["period_kernel"] == 1 and one.info()["list_width"] > 32
+    for n in (79, 250, 3, 170):  # four 80-step periods run as period kernels
+        one.step(n)
+        per_step.step(n)
+        xa, ta = one.state()
+        xb, tb = per_step.state()
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(xa, xb)
+    np.testing.assert_array_equal(one.drift(), per_step.drift())
