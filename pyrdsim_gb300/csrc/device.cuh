@@ -105,7 +105,8 @@ struct SysDev {
   float unit2f;                   // unit^2 as float32
   float delta;                    // allowed displacement since the last
                                   // rebuild (Euclidean, length units)
-  unsigned long long hrange[3];   // high-word range used for cell mapping
+  int hshift[3];                  // cell of high word h: (h * nc) >> hshift
+                                  // (32 periodic, 30 reflecting: h <= 2^30)
   float R2;                       // candidate radius^2 (forces + reactions)
   float Rrx2;                     // reaction radius^2 (guarded)
   float Rl2;                      // Verlet-list radius^2: range + 2 delta

@@ -822,7 +822,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         sd.inv_unit_d[k] = TWO64 / S.L[k];
         sd.unit_hi[k] = (float)(S.L[k] / TWO32);
         sd.inv_unit_hi[k] = (float)(TWO32 / S.L[k]);
-        sd.hrange[k] = 1ULL << 32;
+        sd.hshift[k] = 32;
       } else {
         sd.Si[k] = S_REFLECT;
         hsys.Si[k] = S_REFLECT;
@@ -831,7 +831,7 @@ int rdsim_create(const rdsim_system* systems, int32_t n_systems, const rdsim_opt
         sd.inv_unit_d[k] = (double)S_REFLECT / S.L[k];
         sd.unit_hi[k] = (float)(S.L[k] * TWO32 / (double)S_REFLECT);
         sd.inv_unit_hi[k] = (float)((double)S_REFLECT / (S.L[k] * TWO32));
-        sd.hrange[k] = ((unsigned long long)S_REFLECT >> 32) + 1;
+        sd.hshift[k] = 30;  // high words of [0, 2^62] span [0, 2^30]
       }
       max_unit = std::max(max_unit, (double)sd.unit_hi[k]);
     }

@@ -54,13 +54,15 @@ static __global__ void k_set_counter(long long* c, long long v, int add) {
   else *c = v;
 }
 
-// Cell coordinate along dimension k of high word h.  Reflecting dimensions
-// hold signed values (an initial position may lie below 0 until the first
-// boundary step); those count as cell 0.
+// Cell coordinate along dimension k of high word h: floor(h nc / 2^32) in
+// periodic dimensions, floor(h nc / 2^30) in reflecting ones (their high
+// words span [0, 2^30]; x = L falls into the last cell) -- shifts, no 64-bit
+// division.  Reflecting dimensions hold signed values (an initial position
+// may lie below 0 until the first boundary step); those count as cell 0.
 __device__ inline int cell_coord(const SysDev& s, int k, uint32_t h) {
   unsigned long long v = h;
   if (!((s.periodic >> k) & 1) && (int)h < 0) v = 0;
-  const int c = (int)((v * (unsigned long long)s.nc[k]) / s.hrange[k]);
+  const int c = (int)((v * (unsigned long long)s.nc[k]) >> s.hshift[k]);
   return c >= s.nc[k] ? s.nc[k] - 1 : c;
 }
 
