@@ -933,8 +933,9 @@ __global__ void __launch_bounds__(LBLOCK) k_react_listed(Args a) {
 // theirs bit for bit.
 
 // Polling: relaxed loads (an acquire load invalidates the SM's L1, which
-// the other CTAs on the SM use for their list rows), then one acquire fence
-// once every word has reached its target.
+// the other CTAs on the SM use for their list rows).  With RD_PERIOD_CG = 0
+// (plain loads of other CTAs' words) one acquire fence follows once every
+// word has reached its target; with the default strong loads none does.
 #ifndef RD_PERIOD_POLL_ACQUIRE
 #define RD_PERIOD_POLL_ACQUIRE 0
 #endif
