@@ -67,3 +67,35 @@ def test_struct_sizes_match_header(lib):
 def test_last_error_is_callable_without_gpu(lib):
     lib.rdsim_last_error.restype = ctypes.c_char_p
     assert isinstance(lib.rdsim_last_error(), bytes)
+
+
+def test_option_and_info_layout_match_the_c_compiler(tmp_path):
+    """rdsim_options and rdsim_info as the C compiler lays them out (sizes and
+    the offsets of every field) equal their ctypes mirrors."""
+    import shutil
+    import subprocess
+    from pyrdsim_gb300 import abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = {"rdsim_options": abi.Options, "rdsim_info": abi.Info}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "rdsim.h"', "int main(void) {"]
+    for cname, cls in fields.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)], text=True).split("\n")
+    got = {}
+    for line in out:
+        if line.strip():
+            cname, f, v = line.split()
+            got[(cname, f)] = int(v)
+    for cname, cls in fields.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
