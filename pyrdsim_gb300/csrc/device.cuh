@@ -236,6 +236,9 @@ struct PeriodArgs {
   int nsteps;                     // steps of the rebuild period
   int nchunks;                    // chunks = CTAs (all resident)
   int rx;                         // prefiltered reaction phases run
+  int first_rx;                   // the first step's reactions run here (its
+                                  // candidates from the list builder); 0: done
+                                  // before the launch
   int withhold;                   // test hook: this chunk never publishes
                                   // its progress (-1: none)
   long long wait_ns;              // limit of one wait (global timer, ns)

@@ -525,7 +525,7 @@ int upload_state(rdsim_handle* h) {
 
 int initial_drift(rdsim_handle* h) {
   CK(cudaMemsetAsync(h->rx_count, 0, 3 * sizeof(int), h->stream));
-  int rc = rebuild(h);
+  int rc = rebuild(h, 0, false, false, h->period_on);
   if (rc) return rc;
   rc = force(h, h->step, F_STORE_DRIFT, nullptr);
   if (rc) return rc;
@@ -548,13 +548,18 @@ void launch_period_d(rdsim_handle* h, const Args* A, const PeriodArgs& p) {
   else launch(k_period<D, 4>, g, LBLOCK, h->stream, A[0], A[1], A[2], A[3], p);
 }
 
-// The steps of one rebuild period after its rebuild (which ran with
-// period_prep) as one launch of the period kernel: the drift arguments of
-// steps of parity P read positions xh[cx ^ P] and the types after the
-// step's reactions; the reaction arguments read the types before them.
-// Step numbers are offsets from the device counter.
-int period_launch(rdsim_handle* h, int kf, bool pre) {
-  const int cx0 = h->cx, cm0 = h->cm;
+// Steps of one list period as one launch of the period kernel (the list's
+// last rebuild ran with period_prep): the drift arguments of steps of parity
+// P read positions xh[cx ^ P] and the types after the step's reactions; the
+// reaction arguments read the types before them.  rel: a whole period in a
+// graph capture, step numbers offsets from the device counter, the first
+// step's reactions in the kernel.  Otherwise (the rest of a period after a
+// call started inside it): `nsteps` steps from step `step0`, whose reactions
+// already ran on the reaction kernels.
+int period_launch(rdsim_handle* h, int kf, bool pre, bool rel = true, long long step0 = 0,
+                  int nsteps = 0) {
+  const int cx0 = h->cx;
+  const int cm0 = (!rel && h->has_rx) ? h->cm ^ 1 : h->cm;
   Args A[4];
   for (int P = 0; P < 2; P++) {
     h->cx = cx0 ^ P;
@@ -564,19 +569,23 @@ int period_launch(rdsim_handle* h, int kf, bool pre) {
     Args d = make_args(h);
     d.flags = F_EM | F_CHECK_SKIN | F_PERIOD | kf;
     r.flags = F_PERIOD | kf;
-    d.step_base = r.step_base = h->step_dev;
-    d.step = r.step = 0;
+    d.step_base = r.step_base = rel ? h->step_dev : nullptr;
+    d.step = r.step = rel ? 0 : step0;
     d.wait_ns = r.wait_ns = h->wait_ns;
+    if (!rel) d.stamps = r.stamps = nullptr;  // the timestamps cover whole periods
     A[P] = d;
     A[2 + P] = r;
   }
   h->cx = cx0;
-  h->cm = cm0;
+  h->cm = (!rel && h->has_rx) ? cm0 ^ 1 : cm0;
   PeriodArgs p;
   std::memset(&p, 0, sizeof p);
-  p.nsteps = h->freq;
+  p.nsteps = rel ? h->freq : nsteps;
   p.nchunks = (int)h->chunks_h.size();
   p.rx = pre ? 1 : 0;
+  p.first_rx = rel ? 1 : 0;
+  if (!rel)  // progress words of a launch without the list builder before it
+    CK(cudaMemsetAsync(h->pflag, 0, sizeof(int) * (size_t)p.nchunks * PFLAG_STRIDE, h->stream));
   p.withhold = h->withhold;
   p.wait_ns = h->wait_ns;
   {
@@ -1450,8 +1459,26 @@ int rdsim_step(rdsim_handle* h, int32_t n_steps, int32_t flags, const double* xi
       flagged = false;
       continue;
     }
+    // a call that starts inside a list period: the step's reactions on the
+    // reaction kernels, then the rest of the period in one period-kernel
+    // launch (not when a trajectory frame or the call's last step falls in it)
+    const long long e = (s / h->freq + 1) * h->freq - 1;
+    const int m = (int)(e - s + 1);
+    if (graphable && h->period_on && (pre || !h->has_rx) && s % h->freq != 0 && left > m &&
+        !snapshot_in(h, s, e)) {
+      if (h->has_rx &&
+          (rc = react(h, s, kf, nullptr, nullptr, false, flagged)))
+        return rc;
+      if ((rc = period_launch(h, kf, pre, false, s, m))) return rc;
+      h->cx ^= m & 1;
+      if (h->has_rx) h->cm ^= (m - 1) & 1;
+      h->step = e;
+      q += m;
+      flagged = false;
+      continue;
+    }
     if (s % h->freq == 0) {
-      if ((rc = rebuild(h, s, pre))) return rc;
+      if ((rc = rebuild(h, s, pre, false, h->period_on))) return rc;
       flagged = pre;  // the builder listed this step's candidates
     }
     if (h->has_rx) {

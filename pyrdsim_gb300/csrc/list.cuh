@@ -383,8 +383,9 @@ __device__ inline bool rx_may_react(const SysDev& s, int ti, int cnt, int pid, l
 // F_PERIOD_PREP (CTA = chunk of the period kernel) it also writes the
 // chunk's neighbour-chunk bitmap (the chunks of every list entry, of the
 // bonded partners and the chunk itself), its candidate mask of the rebuild
-// step (instead of the candidate list; their type words carry META_PENDING)
-// and its progress word (0).
+// step (their type words carry META_PENDING until resolved, by the period
+// kernel or by the listed reaction kernel, which also gets the candidate
+// list) and its progress word (0).
 template <int D, int TPP>
 __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Args a) {
   constexpr int PER = LBLOCK / TPP;
@@ -553,7 +554,8 @@ __global__ void __launch_bounds__((LBLOCK / TPP) * (D == 1 ? 1 : 3)) k_nlist(Arg
       a.nbmask[(size_t)c * PMASK_WORDS + w] = sbits[w];
     for (int w = (int)threadIdx.x; w < CAND_WORDS; w += NTH) a.cand0[c * CAND_WORDS + w] = scand[w];
     if (threadIdx.x == 0) a.pflag[c * PFLAG_STRIDE] = 0;
-  } else if (a.flags & F_RX_HERE) {
+  }
+  if (a.flags & F_RX_HERE) {  // the candidate list of the per-step kernels
     const unsigned int bal = __ballot_sync(0xffffffffu, listed);
     if (bal) {
       const int l32 = threadIdx.x & 31, leader = __ffs(bal) - 1;
@@ -1254,7 +1256,7 @@ __global__ void __launch_bounds__(LBLOCK, RD_PERIOD_MIN_BLOCKS)
   long long s0v = 0;
   if (tid == 0) s0v = d0.step_base ? *d0.step_base + d0.step : d0.step;
   uint32_t cw = 0u;
-  if (tid < CAND_WORDS && p.rx) cw = d0.cand0[blockIdx.x * CAND_WORDS + tid];
+  if (tid < CAND_WORDS && p.rx && p.first_rx) cw = d0.cand0[blockIdx.x * CAND_WORDS + tid];
   int pidv = 0;
   uint32_t xrv[3] = {0u, 0u, 0u};
   if (tid < ch.cnt) {
