@@ -337,8 +337,9 @@ int rdsim_get_info(rdsim_handle* h, rdsim_info* info);
  * k_react_listed), 2 = stand-alone Euler-Maruyama (k_em), 3 = cell-list and
  * Verlet-list rebuild (6 kernels), 4 = hooks and observables (the events
  * serialise launches and keep graphs from replaying).  With bit 1 the drift
- * kernel itself records the global timer when each CTA starts its work
- * (after waiting for the previous kernel) and when each of its warps ends; drift_span_ms sums,
+ * kernel itself (the period kernel alone, when rdsim_get_info reports it)
+ * records the global timer when each CTA starts its work (after waiting for
+ * the previous kernel) and when each of its warps ends; drift_span_ms sums,
  * per launch, last end minus first start over the last drift_spans launches
  * (up to 32768 kept), without changing how the step runs (graphs replay). */
 #define RDSIM_PROFILE_CLASSES 5

@@ -382,6 +382,10 @@ int rebuild(rdsim_handle* h, long long step = 0, bool prefilter = false, bool re
 // `rel`: step numbers are offsets from the device counter (graph capture)
 int force(rdsim_handle* h, long long step, int flags, const double* xi_next, bool rel = false) {
   Args a = make_args(h);
+  // with the period kernel on, only its launches record timestamps (one
+  // span per list period; the per-step drift launches at call boundaries
+  // would mix one-step spans into the average)
+  if (h->period_on) a.stamps = nullptr;
   a.step_base = rel ? h->step_dev : nullptr;
   a.step = step;
   a.em_step = step + 1;
